@@ -1,0 +1,253 @@
+/*
+ * tbsla_gb300.h -- C ABI of the GB300 (sm_103a) implementation of TBSLA's
+ * SpMV / a_axpx_ / PageRank path.
+ *
+ * The entry points replace the compute behind TBSLA's tbsla::cpp::Matrix*
+ * classes (src/cpp/include/tbsla/cpp/Matrix.hpp:9-47) and the C_CPP_* C ABI
+ * (src/cpp/interface/c/include/tbsla/cpp/MatrixCSR.h and its siblings).  A
+ * matrix handle owns device
+ * copies of one matrix in the layout its kernels want (CSR with a merge-path
+ * schedule, column-major ELL, row-sorted COO, row-major DENSE).  Plain
+ * pointers and sizes only: no C++ or CUDA types cross this boundary; a
+ * stream is passed as `void*` (a cudaStream_t, NULL for the legacy stream).
+ *
+ * Errors: every call returns a tbsla_status_t; no exception crosses the ABI.
+ * tbsla_last_error() gives a readable message for the calling thread's last
+ * failure.  On TBSLA_ERR_CUDA the handle stays valid only if the CUDA context
+ * does.
+ *
+ * Threading: a handle may be used from several threads for reads (spmv on
+ * device pointers); the *_host entry points use the handle's own stream and
+ * staging buffers and must not run concurrently on one handle.
+ */
+#ifndef TBSLA_GB300_H
+#define TBSLA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TBSLA_OK = 0,
+  TBSLA_ERR_INVALID_ARG = 1,
+  TBSLA_ERR_CUDA = 2,
+  TBSLA_ERR_OOM = 3,
+  TBSLA_ERR_NOT_CONVERGED = 4,
+  TBSLA_ERR_TIMEOUT = 5,
+  TBSLA_ERR_UNSUPPORTED = 6
+} tbsla_status_t;
+
+/* the reference's five storage formats */
+typedef enum {
+  TBSLA_FMT_COO = 0,
+  TBSLA_FMT_SCOO = 1,
+  TBSLA_FMT_CSR = 2,
+  TBSLA_FMT_ELL = 3,
+  TBSLA_FMT_DENSE = 4
+} tbsla_format_t;
+
+/* element types of stored matrix values and of vectors */
+typedef enum { TBSLA_F64 = 0, TBSLA_F32 = 1, TBSLA_BF16 = 2 } tbsla_dtype_t;
+
+/* value-store flags for *_create: which copies of the values to keep on the
+ * device.  F64 is the drop-in; F32 / BF16 are the reduced-precision stores
+ * (products accumulated in FP32). */
+enum { TBSLA_STORE_F64 = 1, TBSLA_STORE_F32 = 2, TBSLA_STORE_BF16 = 4 };
+
+typedef struct tbsla_matrix tbsla_matrix_t;
+
+typedef struct {
+  int format;          /* tbsla_format_t */
+  int n_row, n_col;    /* global shape (Matrix::get_n_row/get_n_col)       */
+  int f_row, f_col;    /* first row / column of the stored block           */
+  int rows;            /* rows the kernels visit (rows past it give 0)     */
+  int max_col;         /* ELL width                                        */
+  int64_t stored;      /* stored entries (ELL: rows*max_col, DENSE: rows*cols) */
+  int stores;          /* TBSLA_STORE_* bits present                       */
+  int64_t device_bytes;/* device memory held by the handle                 */
+} tbsla_matrix_info_t;
+
+/* ---------------------------------------------------------------- misc */
+const char *tbsla_last_error(void);
+const char *tbsla_status_string(tbsla_status_t s);
+int tbsla_version(void);
+/* device the library uses for new handles (default: current device) */
+tbsla_status_t tbsla_set_device(int device);
+
+/* ------------------------------------------------------------ matrices */
+/* CSR from host arrays.  Replaces MatrixCSR(n_row, n_col, values, rowptr,
+ * colidx) (src/cpp/include/tbsla/cpp/MatrixCSR.hpp:15, MatrixCSR.cpp:13-27)
+ * and the storage behind MatrixCSR::spmv (MatrixCSR.cpp:123-140).  rowptr has
+ * rows+1 entries; its first entry is the base subtracted from every other
+ * entry (the reference's rowptr.front()).  colidx holds global columns; the
+ * kernel reads x[colidx - f_col].  rows may be below n_row (rows past it give
+ * y = 0, as when the reference's rowptr is shorter than n_row+1). */
+tbsla_status_t tbsla_csr_create(int n_row, int n_col, int f_col, int rows, const int *rowptr,
+                                const int *colidx, const double *values, int stores,
+                                tbsla_matrix_t **out);
+
+/* ELL from host arrays in the reference's row-major layout
+ * (values[i*max_col + j], columns[i*max_col + j], MatrixELL.hpp:33-35).
+ * rows = min(ln_row, values.size()/max_col) as MatrixELL::Ax visits
+ * (MatrixELL.cpp:101-114); padding is (column 0, value 0) and a column below
+ * f_col is read as x[0], exactly as the reference clamps it.  Stored on the
+ * device column-major. */
+tbsla_status_t tbsla_ell_create(int n_row, int n_col, int f_col, int rows, int max_col,
+                                const int *columns, const double *values, int stores,
+                                tbsla_matrix_t **out);
+
+/* COO / SCOO from host triplets.  Replaces MatrixCOO(n_row, n_col, values,
+ * row, col) (MatrixCOO.hpp:14, MatrixCOO.cpp:30-44) and MatrixSCOO's
+ * (MatrixSCOO.hpp:15); spmv adds values[k]*x[col[k]-f_col] into
+ * y[row[k]-f_row] as MatrixCOO::Ax / MatrixSCOO::Ax do (MatrixCOO.cpp:107-116,
+ * MatrixSCOO.cpp:114-123).  COO passes f_row = f_col = 0.  Entries are put in
+ * row order (stable) at creation; entries whose output row falls outside
+ * [0, n_row) are rejected with TBSLA_ERR_INVALID_ARG. */
+tbsla_status_t tbsla_coo_create(int n_row, int n_col, int f_row, int f_col, int64_t nnz,
+                                const int *row, const int *col, const double *values, int stores,
+                                tbsla_matrix_t **out);
+
+/* DENSE row-major ln_row x ln_col block (MatrixDENSE.hpp:33, Ax at
+ * MatrixDENSE.cpp:64-73); y has n_row entries, rows past ln_row give 0. */
+tbsla_status_t tbsla_dense_create(int n_row, int n_col, int ln_row, int ln_col,
+                                  const double *values, int stores, tbsla_matrix_t **out);
+
+tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A);
+tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
+
+/* --------------------------------------------------------------- SpMV */
+/* y[0:n_row] = A x on device pointers, ordered on `stream`; FP64 vectors and
+ * FP64 values.  x has n_col - f_col... entries addressed as x[col - f_col]
+ * (the reference's v[colidx - f_col]).  Replaces Matrix::spmv
+ * (Matrix.hpp:12) / Ax (Matrix.hpp:13).  vect_incr shifts COO/SCOO output
+ * rows (MatrixCOO.cpp:114); rows shifted outside [0, n_row) are dropped.  */
+tbsla_status_t tbsla_spmv(const tbsla_matrix_t *A, const double *d_x, double *d_y, int vect_incr,
+                          void *stream);
+
+/* General form: values read from the `store` copy (TBSLA_F64/F32/BF16);
+ * x and y in x_type / y_type (TBSLA_F64 or TBSLA_F32).  Products accumulate
+ * in FP64 for the F64 store and in FP32 for the F32/BF16 stores. */
+tbsla_status_t tbsla_spmv_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_dtype_t x_type,
+                             const void *d_x, tbsla_dtype_t y_type, void *d_y, int vect_incr,
+                             void *stream);
+
+/* Synchronous host-vector form used by the drop-in classes
+ * (std::vector<double> in, std::vector<double> out): copies x (nx entries)
+ * to the device, runs tbsla_spmv, copies y (ny >= n_row entries) back. */
+tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *y,
+                               int64_t ny, int vect_incr);
+
+/* r = A (A x + x): Matrix::a_axpx_ (Matrix.cpp:6-11), square matrices; the
+ * "+ x" is fused into the first product.  d_tmp: n_row doubles of scratch or
+ * NULL to use the handle's own. */
+tbsla_status_t tbsla_a_axpx(const tbsla_matrix_t *A, const double *d_x, double *d_r,
+                            double *d_tmp, int vect_incr, void *stream);
+tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *r,
+                                 int64_t nr, int vect_incr);
+
+/* ----------------------------------------------------------- PageRank */
+typedef enum {
+  /* Matrix::page_rank (Matrix.cpp:13-61): b0 = 1; b = beta*A b + (1-beta)/n *
+   * sum(b_prev); b /= max(b); stop when sum|b - b_prev| < tol; finally
+   * b /= sum(b).  No dangling term. */
+  TBSLA_PR_REFERENCE = 0,
+  /* x0 = 1/n; x = beta*A x + (beta*dangling(x) + (1-beta)*sum(x))/n, where
+   * dangling(x) sums x over columns of A with no stored entry; stop when
+   * ||x - x_prev||_1 < tol.  Result sums to 1. */
+  TBSLA_PR_DANGLING = 1
+} tbsla_pr_mode_t;
+
+typedef struct {
+  double beta;        /* damping, the reference's beta                     */
+  double tol;         /* stopping threshold, the reference's epsilon       */
+  int max_iter;       /* the reference's max_iteration                     */
+  int mode;           /* tbsla_pr_mode_t                                   */
+  int precision;      /* TBSLA_F64: plain FP64 sweeps.  TBSLA_F32 / TBSLA_BF16:
+                         low-precision sweeps on that value store with FP32
+                         vectors, corrected by FP64 residual refinement
+                         (TBSLA_PR_DANGLING only; needs TBSLA_STORE_F64 too) */
+  int check_every;    /* sweeps per convergence check (0: library default) */
+} tbsla_pagerank_params_t;
+
+typedef struct {
+  int iterations;     /* sweeps done (FP64 + low precision)                */
+  int iterations_f64; /* of which FP64 sweeps                              */
+  double residual;    /* last stopping quantity                            */
+  int converged;      /* 1 if tol was reached                              */
+} tbsla_pagerank_result_t;
+
+/* d_out: n_col doubles on the device.  Returns TBSLA_OK also when max_iter
+ * is hit without convergence (as the reference does); check
+ * result->converged. */
+tbsla_status_t tbsla_pagerank(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                              double *d_out, tbsla_pagerank_result_t *result, void *stream);
+tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                   double *out, int64_t n_out, tbsla_pagerank_result_t *result);
+
+/* Matrix::personalized_page_rank (Matrix.cpp:63-114): as TBSLA_PR_REFERENCE
+ * with b0 = 0.25 and the teleport term (1-beta)*sum(b_prev)/n_nodes added only
+ * to the listed nodes (a node listed twice counts once but n_nodes is the
+ * list length, as std::find over the list gives). */
+tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                                const int *nodes, int n_nodes, double *out,
+                                                int64_t n_out, tbsla_pagerank_result_t *result);
+
+/* ---------------------------------------------------------- generators */
+/* Host-side builders of the reference's synthetic matrices, in the
+ * reference's own array layout, so that the drop-in classes and the C_CPP_*
+ * ABI return exactly the reference's arrays.  Two-call protocol: call with
+ * NULL arrays to get the sizes in *sizes, allocate, call again.
+ *   sizes[0] = values length, sizes[1] = idx0 length (row / rowptr /
+ *   columns), sizes[2] = idx1 length (col / colidx)
+ *   geom[0..10] = n_row, n_col, ln_row, ln_col, f_row, f_col, pr, pc, NR, NC,
+ *   max_col;  *nnz = the reference's nnz field.
+ * gen: 0 = cqmat (Matrix*::fill_cqmat), 1 = cdiag (fill_cdiag),
+ *      2 = cqmat_stochastic (fill_cqmat_stochastic). */
+tbsla_status_t tbsla_generate(int format, int gen, int n_row, int n_col, int c, double q,
+                              unsigned int seed_mult, int pr, int pc, int NR, int NC,
+                              int64_t sizes[3], int geom[11], int64_t *nnz, double *values,
+                              int *idx0, int *idx1);
+
+/* One-pass form: builds the block (pr,pc,NR,NC) = (0,0,1,1) of the chosen
+ * generator and uploads it as a handle of `format` with the given value
+ * stores (the matrices tbsla_perf times, src/cpp/apps/tbsla_perf.cpp:111-119). */
+tbsla_status_t tbsla_generate_matrix(int format, int gen, int n_row, int n_col, int c, double q,
+                                     unsigned int seed_mult, int stores, tbsla_matrix_t **out);
+
+/* R-MAT digraph with 2^scale nodes and m edge draws (Chakrabarti, Zhan,
+ * Faloutsos 2004), generated on the device with counter-based draws, as the
+ * column-stochastic PageRank matrix: row = destination, column = source,
+ * repeated edges merged, value 1/outdeg(source).  The product is a CSR
+ * handle with the requested value stores. */
+tbsla_status_t tbsla_rmat_pagerank_matrix(int scale, int64_t m, double a, double b, double c,
+                                          uint64_t seed, int stores, tbsla_matrix_t **out);
+/* host copy of a CSR handle's arrays (rowptr rows+1, colidx/values nnz) */
+tbsla_status_t tbsla_csr_download(const tbsla_matrix_t *A, int *rowptr, int *colidx,
+                                  double *values);
+
+/* ---------------------------------------------------------- utilities */
+/* sizes of device buffers; simple wrappers so that C callers need no CUDA
+ * headers */
+tbsla_status_t tbsla_device_alloc(void **ptr, size_t bytes);
+tbsla_status_t tbsla_device_free(void *ptr);
+tbsla_status_t tbsla_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
+tbsla_status_t tbsla_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+tbsla_status_t tbsla_stream_sync(void *stream);
+/* page-locked host buffers (fast host<->device copies for the *_host calls) */
+tbsla_status_t tbsla_host_alloc(void **ptr, size_t bytes);
+tbsla_status_t tbsla_host_free(void *ptr);
+
+/* Kernel timing: when enabled, every product launched on A records CUDA
+ * events around its main kernel on the launching stream; the accumulated
+ * device time and launch count are read (synchronising on the events) and
+ * reset with tbsla_kernel_timing_read. */
+tbsla_status_t tbsla_kernel_timing_enable(tbsla_matrix_t *A, int enable);
+tbsla_status_t tbsla_kernel_timing_read(tbsla_matrix_t *A, double *total_ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

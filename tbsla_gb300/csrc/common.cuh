@@ -1,0 +1,153 @@
+// common.cuh -- shared definitions of the tbsla_gb300 library: the matrix
+// handle, error reporting, and small device helpers.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/tbsla_gb300.h"
+
+namespace tbsla {
+
+// ---------------------------------------------------------------- errors
+tbsla_status_t fail(tbsla_status_t s, const char *fmt, ...);
+tbsla_status_t cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define TB_CUDA(call)                                                           \
+  do {                                                                          \
+    cudaError_t tb_e_ = (call);                                                 \
+    if (tb_e_ != cudaSuccess) return ::tbsla::cuda_fail(tb_e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define TB_CHECK(cond, ...)                                                     \
+  do {                                                                          \
+    if (!(cond)) return ::tbsla::fail(TBSLA_ERR_INVALID_ARG, __VA_ARGS__);      \
+  } while (0)
+
+#define TB_TRY(...)                                                             \
+  do {                                                                          \
+    tbsla_status_t tb_s_ = (__VA_ARGS__);                                       \
+    if (tb_s_ != TBSLA_OK) return tb_s_;                                        \
+  } while (0)
+
+// ------------------------------------------------------------- constants
+// merge-path tiling of CSR / COO: threads per CTA and items per thread.
+// Items per thread is odd so that consecutive-item shared-memory reads of 4-
+// and 8-byte words are free of bank conflicts.
+constexpr int kMergeThreads = 256;
+constexpr int kMergeItems = 9;
+constexpr int kMergeTile = kMergeThreads * kMergeItems;
+
+// -------------------------------------------------------------- handle
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace tbsla
+
+// The opaque matrix handle of the C ABI.
+struct tbsla_matrix {
+  int format = 0;
+  int n_row = 0, n_col = 0;
+  int f_row = 0, f_col = 0;
+  int rows = 0;          // rows visited by the kernels
+  int cols = 0;          // DENSE: ln_col
+  int max_col = 0;       // ELL width
+  int64_t stored = 0;    // stored entries
+  int stores = 0;        // TBSLA_STORE_* bits
+  int device = 0;
+
+  // values in up to three precisions (F64, F32, BF16), same positions
+  void *values[3] = {nullptr, nullptr, nullptr};
+  // CSR: row_end (rows ints, base removed); ELL: column-major columns
+  // (rows_pad * max_col); COO: row (stored)
+  int *idx0 = nullptr;
+  // CSR: colidx; COO: col
+  int *idx1 = nullptr;
+  int rows_pad = 0;      // ELL: padded row count of the column-major arrays
+  int64_t x_extent = 0;  // entries of x the kernels read (max column - f_col + 1)
+
+  // merge-path schedule (CSR, COO): tile start coordinates and carries
+  int num_tiles = 0;
+  int2 *tile_start = nullptr;   // CSR: (row, nnz) at each tile start, num_tiles+1
+  int *tile_head_row = nullptr; // per tile: row continued from an earlier tile, or -1
+  double *tile_head_val = nullptr;
+  double *tile_tail_val = nullptr;
+  unsigned char *tile_emitted = nullptr;
+  float *tile_head_val32 = nullptr;  // FP32-accumulating variants
+  float *tile_tail_val32 = nullptr;
+
+  // PageRank helpers built on first use
+  unsigned char *dangling = nullptr;  // columns without stored entries
+  double *pr_scratch = nullptr;       // reduction partials and scalars
+  size_t pr_scratch_bytes = 0;
+
+  // host-path staging
+  cudaStream_t stream = nullptr;
+  double *d_x = nullptr, *d_y = nullptr, *d_t = nullptr;
+  int64_t cap_x = 0, cap_y = 0, cap_t = 0;
+
+  int64_t device_bytes = 0;
+  std::mutex host_mu;
+
+  // optional per-launch timing of the main product kernel
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending_events;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> free_events;
+  double timed_ms = 0;
+  int64_t timed_launches = 0;
+};
+
+namespace tbsla {
+
+tbsla_status_t dev_alloc(tbsla_matrix *A, void **p, size_t bytes);
+// brackets the main kernel of a product when A->timing is set
+struct KernelTimer {
+  tbsla_matrix *A;
+  cudaStream_t s;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  KernelTimer(const tbsla_matrix *A_, cudaStream_t s_);
+  void stop();
+};
+tbsla_status_t ensure_host_buffers(tbsla_matrix *A, int64_t nx, int64_t ny, int64_t nt);
+int current_device();
+
+inline int store_index(tbsla_dtype_t t) { return t == TBSLA_F64 ? 0 : (t == TBSLA_F32 ? 1 : 2); }
+
+// ------------------------------------------------------- device helpers
+template <typename T> struct AccOf { using type = float; };
+template <> struct AccOf<double> { using type = double; };
+
+__device__ __forceinline__ double to_acc(double v, double) { return v; }
+__device__ __forceinline__ float to_acc(float v, float) { return v; }
+__device__ __forceinline__ float to_acc(__nv_bfloat16 v, float) { return __bfloat162float(v); }
+__device__ __forceinline__ float to_acc(double v, float) { return (float)v; }
+__device__ __forceinline__ double to_acc(float v, double) { return (double)v; }
+
+// fused multiply-add in the accumulator type
+__device__ __forceinline__ double fma_acc(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_acc(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// streaming loads of matrix data (read once: evict-first in L2 so that the
+// gathered vector stays resident)
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+template <> __device__ __forceinline__ __nv_bfloat16 ld_stream(const __nv_bfloat16 *p) {
+  unsigned short u = __ldcs(reinterpret_cast<const unsigned short *>(p));
+  return __ushort_as_bfloat16(u);
+}
+
+// gathered vector loads (read-only path)
+template <typename T> __device__ __forceinline__ T ld_vec(const T *p) { return __ldg(p); }
+
+template <typename T> __device__ __forceinline__ void st_out(T *p, double v) { *p = (T)v; }
+template <typename T> __device__ __forceinline__ void st_out(T *p, float v) { *p = (T)v; }
+
+}  // namespace tbsla

@@ -1,0 +1,31 @@
+// host_gen.h -- C++ interface of the synthetic-matrix builders, used by the
+// drop-in classes (arrays straight into their std::vectors) and by
+// tbsla_generate / tbsla_generate_matrix.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/tbsla_gb300.h"
+
+namespace tbsla {
+
+struct GenArrays {
+  int format = 0;
+  // n_row n_col ln_row ln_col f_row f_col pr pc NR NC max_col
+  int geom[11] = {0};
+  int64_t nnz = 0;
+  bool nnz_set = false;  // false where the reference leaves nnz unset
+  std::vector<double> values;
+  std::vector<int> idx0, idx1;
+};
+
+// gen: 0 = cqmat, 1 = cdiag (c is the diagonal offset), 2 = cqmat_stochastic
+tbsla_status_t generate_arrays(int format, int gen, int n_row, int n_col, int c, double q,
+                               unsigned int seed_mult, int pr, int pc, int NR, int NC,
+                               GenArrays &out);
+
+// column sums of the global cqmat (values_generation.cpp:47-62)
+std::vector<double> cqmat_column_sums(int n_row, int n_col, int c, double q, unsigned int seed_mult);
+
+}  // namespace tbsla

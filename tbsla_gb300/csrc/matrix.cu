@@ -1,0 +1,680 @@
+// matrix.cu -- matrix handles of the C ABI: creation from host arrays in the
+// reference's layouts, device layouts, SpMV / a_axpx dispatch.
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "spmv_kernels.cuh"
+
+namespace tbsla {
+
+// ------------------------------------------------------------- errors
+static thread_local std::string g_err;
+static int g_device = -1;
+
+tbsla_status_t fail(tbsla_status_t s, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return s;
+}
+
+tbsla_status_t cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  const tbsla_status_t s = e == cudaErrorMemoryAllocation ? TBSLA_ERR_OOM : TBSLA_ERR_CUDA;
+  return fail(s, "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+int current_device() {
+  int d = 0;
+  if (g_device >= 0) return g_device;
+  cudaGetDevice(&d);
+  return d;
+}
+
+tbsla_status_t dev_alloc(tbsla_matrix *A, void **p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  // 16 spare bytes so that vector loads of a ragged end stay inside
+  cudaError_t e = cudaMalloc(p, bytes + 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(TBSLA_ERR_OOM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  if (A) A->device_bytes += (int64_t)bytes + 16;
+  return TBSLA_OK;
+}
+
+KernelTimer::KernelTimer(const tbsla_matrix *A_, cudaStream_t s_) : A(const_cast<tbsla_matrix *>(A_)), s(s_) {
+  if (!A || !A->timing) return;
+  if (!A->free_events.empty()) {
+    e0 = A->free_events.back().first;
+    e1 = A->free_events.back().second;
+    A->free_events.pop_back();
+  } else if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    e0 = e1 = nullptr;
+    return;
+  }
+  cudaEventRecord(e0, s);
+}
+
+void KernelTimer::stop() {
+  if (!e0) return;
+  cudaEventRecord(e1, s);
+  A->pending_events.emplace_back(e0, e1);
+  e0 = e1 = nullptr;
+}
+
+template <typename T> static tbsla_status_t alloc_n(tbsla_matrix *A, T **p, int64_t n) {
+  return dev_alloc(A, reinterpret_cast<void **>(p), (size_t)std::max<int64_t>(n, 1) * sizeof(T));
+}
+
+tbsla_status_t ensure_host_buffers(tbsla_matrix *A, int64_t nx, int64_t ny, int64_t nt) {
+  if (!A->stream) TB_CUDA(cudaStreamCreateWithFlags(&A->stream, cudaStreamNonBlocking));
+  if (nx > A->cap_x) {
+    if (A->d_x) cudaFree(A->d_x);
+    A->d_x = nullptr;
+    TB_TRY(alloc_n(A, &A->d_x, nx));
+    A->cap_x = nx;
+  }
+  if (ny > A->cap_y) {
+    if (A->d_y) cudaFree(A->d_y);
+    A->d_y = nullptr;
+    TB_TRY(alloc_n(A, &A->d_y, ny));
+    A->cap_y = ny;
+  }
+  if (nt > A->cap_t) {
+    if (A->d_t) cudaFree(A->d_t);
+    A->d_t = nullptr;
+    TB_TRY(alloc_n(A, &A->d_t, nt));
+    A->cap_t = nt;
+  }
+  return TBSLA_OK;
+}
+
+// ------------------------------------------------------- value stores
+__global__ void f64_to_f32_kernel(const double *in, float *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __double2float_rn(in[i]);
+}
+__global__ void f64_to_bf16_kernel(const double *in, __nv_bfloat16 *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __double2bfloat16(in[i]);
+}
+
+static int grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32);
+}
+
+// Uploads n FP64 values and derives the requested reduced stores on the
+// device.  `host` may hold the values in any order the caller prepared.
+static tbsla_status_t upload_values(tbsla_matrix *A, const double *host, int64_t n, int stores) {
+  if (!(stores & (TBSLA_STORE_F64 | TBSLA_STORE_F32 | TBSLA_STORE_BF16)))
+    return fail(TBSLA_ERR_INVALID_ARG, "no value store requested");
+  double *d64 = nullptr;
+  TB_TRY(alloc_n(A, &d64, n));
+  if (n) TB_CUDA(cudaMemcpy(d64, host, n * sizeof(double), cudaMemcpyHostToDevice));
+  if (stores & TBSLA_STORE_F32) {
+    float *d = nullptr;
+    TB_TRY(alloc_n(A, &d, n));
+    if (n) f64_to_f32_kernel<<<grid_for(n, 256), 256>>>(d64, d, n);
+    A->values[1] = d;
+  }
+  if (stores & TBSLA_STORE_BF16) {
+    __nv_bfloat16 *d = nullptr;
+    TB_TRY(alloc_n(A, &d, n));
+    if (n) f64_to_bf16_kernel<<<grid_for(n, 256), 256>>>(d64, d, n);
+    A->values[2] = d;
+  }
+  TB_CUDA(cudaGetLastError());
+  if (stores & TBSLA_STORE_F64) {
+    A->values[0] = d64;
+  } else {
+    TB_CUDA(cudaDeviceSynchronize());
+    cudaFree(d64);
+    A->device_bytes -= (int64_t)std::max<int64_t>(n, 1) * 8 + 16;
+  }
+  A->stores = stores & (TBSLA_STORE_F64 | TBSLA_STORE_F32 | TBSLA_STORE_BF16);
+  return TBSLA_OK;
+}
+
+// ------------------------------------------------- merge-path schedule
+// tile_start[t] = merge-path coordinate (row, nonzero) of diagonal t*TILE
+__global__ void csr_schedule_kernel(const int *row_end, int rows, int nnz, int num_tiles,
+                                    int2 *tile_start) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > num_tiles) return;
+  const int64_t full = (int64_t)t * kMergeTile, end = (int64_t)rows + nnz;
+  const int d = (int)(full < end ? full : end);
+  int lo = max(d - nnz, 0), hi = min(d, rows);
+  while (lo < hi) {
+    const int p = (lo + hi) >> 1;
+    if (row_end[p] <= d - p - 1) lo = p + 1; else hi = p;
+  }
+  tile_start[t] = make_int2(lo, d - lo);
+}
+
+static tbsla_status_t alloc_carries(tbsla_matrix *A) {
+  const int nt = std::max(A->num_tiles, 1);
+  TB_TRY(alloc_n(A, &A->tile_head_row, nt));
+  TB_TRY(alloc_n(A, &A->tile_head_val, nt));
+  TB_TRY(alloc_n(A, &A->tile_tail_val, nt));
+  TB_TRY(alloc_n(A, &A->tile_emitted, nt));
+  TB_TRY(alloc_n(A, &A->tile_head_val32, nt));
+  TB_TRY(alloc_n(A, &A->tile_tail_val32, nt));
+  return TBSLA_OK;
+}
+
+static tbsla_matrix *new_handle(int format) {
+  tbsla_matrix *A = new (std::nothrow) tbsla_matrix();
+  if (!A) return nullptr;
+  A->format = format;
+  A->device = current_device();
+  cudaSetDevice(A->device);
+  return A;
+}
+
+static void free_handle(tbsla_matrix *A) {
+  if (!A) return;
+  cudaSetDevice(A->device);
+  for (void *p : A->values) if (p) cudaFree(p);
+  void *ptrs[] = {A->idx0, A->idx1, A->tile_start, A->tile_head_row, A->tile_head_val,
+                  A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
+                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t};
+  for (void *p : ptrs) if (p) cudaFree(p);
+  if (A->stream) cudaStreamDestroy(A->stream);
+  for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto &e : A->free_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  delete A;
+}
+
+tbsla_status_t axpy_inplace(double *y, const double *x, int64_t n, cudaStream_t s);
+
+template <typename Acc> Carry<Acc> carry_of(const tbsla_matrix *A);
+template <> Carry<double> carry_of<double>(const tbsla_matrix *A) {
+  return Carry<double>{A->tile_head_row, A->tile_head_val, A->tile_tail_val, A->tile_emitted};
+}
+template <> Carry<float> carry_of<float>(const tbsla_matrix *A) {
+  return Carry<float>{A->tile_head_row, A->tile_head_val32, A->tile_tail_val32, A->tile_emitted};
+}
+
+// ------------------------------------------------------------ launches
+template <typename V, typename XT, typename Epi>
+tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x, Epi epi,
+                              cudaStream_t s) {
+  using Acc = typename Epi::Acc;
+  switch (A->format) {
+  case TBSLA_FMT_CSR:
+    if (A->rows > 0) {
+      KernelTimer kt(A, s);
+      csr_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
+          A->idx0, A->idx1, vals, x, A->f_col, A->rows, A->tile_start, carry_of<Acc>(A), epi);
+      kt.stop();
+      merge_fixup_kernel<Epi><<<(A->num_tiles + 255) / 256, 256, 0, s>>>(A->num_tiles, carry_of<Acc>(A), epi);
+    }
+    break;
+  case TBSLA_FMT_COO:
+  case TBSLA_FMT_SCOO:
+    if (A->stored > 0) {
+      KernelTimer kt(A, s);
+      coo_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
+          A->idx0, A->idx1, vals, x, A->f_col, A->stored, carry_of<Acc>(A), epi);
+      kt.stop();
+      merge_fixup_kernel<Epi><<<(A->num_tiles + 255) / 256, 256, 0, s>>>(A->num_tiles, carry_of<Acc>(A), epi);
+    }
+    break;
+  case TBSLA_FMT_ELL:
+    if (A->rows > 0 && A->max_col > 0) {
+      const int threads = (A->rows + 3) / 4;
+      KernelTimer kt(A, s);
+      ell_kernel<V, XT, Epi><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                 A->rows_pad, A->max_col, epi);
+      kt.stop();
+    }
+    break;
+  case TBSLA_FMT_DENSE:
+    if (A->rows > 0 && A->cols > 0) {
+      const int warps = (A->rows + 3) / 4;
+      KernelTimer kt(A, s);
+      dense_kernel<V, XT, Epi><<<(warps + 7) / 8, 256, 0, s>>>(vals, x, A->rows, A->cols, epi);
+      kt.stop();
+    }
+    break;
+  default:
+    return fail(TBSLA_ERR_INVALID_ARG, "unknown format %d", A->format);
+  }
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// y rows the format never writes are zeroed first: COO/SCOO rows without
+// entries, CSR/ELL/DENSE rows past A->rows, and everything when the
+// reference's early exits apply
+static tbsla_status_t zero_unwritten(const tbsla_matrix *A, void *y, size_t elt, int vect_incr,
+                                     cudaStream_t s) {
+  if (A->n_row <= 0) return TBSLA_OK;
+  if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO) {
+    TB_CUDA(cudaMemsetAsync(y, 0, (size_t)A->n_row * elt, s));
+    return TBSLA_OK;
+  }
+  (void)vect_incr;
+  int written = A->rows;
+  if (A->format == TBSLA_FMT_ELL && A->max_col == 0) written = 0;
+  if (A->format == TBSLA_FMT_DENSE && A->cols == 0) written = 0;
+  if (A->format == TBSLA_FMT_CSR && A->stored == 0) written = 0;
+  written = std::min(written, A->n_row);
+  if (written < A->n_row)
+    TB_CUDA(cudaMemsetAsync(static_cast<char *>(y) + (size_t)written * elt, 0,
+                            (size_t)(A->n_row - written) * elt, s));
+  return TBSLA_OK;
+}
+
+static int out_shift(const tbsla_matrix *A, int vect_incr) {
+  if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO) return vect_incr - A->f_row;
+  return 0;
+}
+
+template <typename V, typename XT, typename YT>
+static tbsla_status_t spmv_typed(const tbsla_matrix *A, const V *vals, const XT *x, YT *y,
+                                 int vect_incr, cudaStream_t s) {
+  using Acc = typename AccOf<V>::type;
+  TB_TRY(zero_unwritten(A, y, sizeof(YT), vect_incr, s));
+  if (A->format == TBSLA_FMT_CSR && A->stored == 0) return TBSLA_OK;  // MatrixCSR.cpp:130-131
+  StoreEpi<YT, Acc> epi{y, A->n_row, out_shift(A, vect_incr)};
+  return launch_product<V, XT>(A, vals, x, epi, s);
+}
+
+tbsla_status_t spmv_dispatch(const tbsla_matrix *A, tbsla_dtype_t store, tbsla_dtype_t xt,
+                             const void *x, tbsla_dtype_t yt, void *y, int vect_incr,
+                             cudaStream_t s) {
+  const int si = store_index(store);
+  const void *vals = A->values[si];
+  if (!vals) return fail(TBSLA_ERR_INVALID_ARG, "value store %d not present in this handle", (int)store);
+  if (xt != TBSLA_F64 && xt != TBSLA_F32) return fail(TBSLA_ERR_INVALID_ARG, "x type must be F64 or F32");
+  if (yt != TBSLA_F64 && yt != TBSLA_F32) return fail(TBSLA_ERR_INVALID_ARG, "y type must be F64 or F32");
+#define TB_SPMV_CASE(VT)                                                                          \
+  {                                                                                               \
+    const VT *v = static_cast<const VT *>(vals);                                                  \
+    if (xt == TBSLA_F64 && yt == TBSLA_F64)                                                       \
+      return spmv_typed(A, v, static_cast<const double *>(x), static_cast<double *>(y), vect_incr, s); \
+    if (xt == TBSLA_F32 && yt == TBSLA_F32)                                                       \
+      return spmv_typed(A, v, static_cast<const float *>(x), static_cast<float *>(y), vect_incr, s); \
+    if (xt == TBSLA_F64 && yt == TBSLA_F32)                                                       \
+      return spmv_typed(A, v, static_cast<const double *>(x), static_cast<float *>(y), vect_incr, s); \
+    return spmv_typed(A, v, static_cast<const float *>(x), static_cast<double *>(y), vect_incr, s); \
+  }
+  if (si == 0) TB_SPMV_CASE(double)
+  if (si == 1) TB_SPMV_CASE(float)
+  TB_SPMV_CASE(__nv_bfloat16)
+#undef TB_SPMV_CASE
+}
+
+tbsla_status_t a_axpx_dispatch(const tbsla_matrix *A, const double *x, double *r, double *tmp,
+                               int vect_incr, cudaStream_t s) {
+  const double *vals = static_cast<const double *>(A->values[0]);
+  if (!vals) return fail(TBSLA_ERR_INVALID_ARG, "a_axpx needs the F64 value store");
+  // tmp = A x + x (rows never written by the product stay x, as r(0)+v)
+  TB_TRY(zero_unwritten(A, tmp, sizeof(double), vect_incr, s));
+  const bool empty = (A->format == TBSLA_FMT_CSR && A->stored == 0);
+  if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO || empty || A->rows < A->n_row ||
+      (A->format == TBSLA_FMT_ELL && A->max_col == 0) || (A->format == TBSLA_FMT_DENSE && A->cols == 0)) {
+    // rows without a product still get "+ x": run the plain product, then add
+    if (!empty) {
+      StoreEpi<double, double> epi{tmp, A->n_row, out_shift(A, vect_incr)};
+      TB_TRY(launch_product<double, double>(A, vals, x, epi, s));
+    }
+    // tmp += x
+    TB_TRY(axpy_inplace(tmp, x, A->n_row, s));
+  } else {
+    AddXEpi<double> epi{tmp, x, A->n_row, out_shift(A, vect_incr)};
+    TB_TRY(launch_product<double, double>(A, vals, x, epi, s));
+  }
+  return spmv_typed<double, double, double>(A, vals, tmp, r, vect_incr, s);
+}
+
+__global__ void axpy_kernel(double *y, const double *x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += x[i];
+}
+tbsla_status_t axpy_inplace(double *y, const double *x, int64_t n, cudaStream_t s) {
+  if (n <= 0) return TBSLA_OK;
+  axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, x, n);
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// ------------------------------------------------------------ creation
+static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *colidx,
+                                const double *values, int stores) {
+  const int rows = A->rows;
+  const int base = rows >= 0 ? rowptr[0] : 0;
+  const int64_t nnz = (int64_t)rowptr[rows] - base;
+  if (nnz < 0 || nnz > INT_MAX) return fail(TBSLA_ERR_INVALID_ARG, "bad rowptr range");
+  std::vector<int> row_end((size_t)std::max(rows, 1));
+  int prev = base;
+  for (int i = 0; i < rows; ++i) {
+    const int e = rowptr[i + 1];
+    if (e < prev) return fail(TBSLA_ERR_INVALID_ARG, "rowptr is not monotone at row %d", i);
+    row_end[i] = e - base;
+    prev = e;
+  }
+  if ((int64_t)rows + nnz > INT_MAX) return fail(TBSLA_ERR_INVALID_ARG, "rows + nnz exceeds the 32-bit index range");
+  int cmax = -1;
+  for (int64_t k = 0; k < nnz; ++k) {
+    const int c = colidx[k] - A->f_col;
+    if (c < 0 || c >= A->n_col) return fail(TBSLA_ERR_INVALID_ARG, "colidx[%lld]=%d outside the column block", (long long)k, colidx[k]);
+    cmax = std::max(cmax, c);
+  }
+  A->x_extent = cmax + 1;
+  A->stored = nnz;
+  TB_TRY(alloc_n(A, &A->idx0, rows));
+  TB_TRY(alloc_n(A, &A->idx1, nnz));
+  if (rows) TB_CUDA(cudaMemcpy(A->idx0, row_end.data(), rows * sizeof(int), cudaMemcpyHostToDevice));
+  if (nnz) TB_CUDA(cudaMemcpy(A->idx1, colidx, nnz * sizeof(int), cudaMemcpyHostToDevice));
+  TB_TRY(upload_values(A, values, nnz, stores));
+  const int64_t items = (int64_t)rows + nnz;
+  A->num_tiles = (int)((items + kMergeTile - 1) / kMergeTile);
+  TB_TRY(alloc_n(A, &A->tile_start, A->num_tiles + 1));
+  csr_schedule_kernel<<<(A->num_tiles + 1 + 255) / 256, 256>>>(A->idx0, rows, (int)nnz, A->num_tiles, A->tile_start);
+  TB_CUDA(cudaGetLastError());
+  TB_TRY(alloc_carries(A));
+  TB_CUDA(cudaDeviceSynchronize());
+  return TBSLA_OK;
+}
+
+}  // namespace tbsla
+
+using namespace tbsla;
+
+extern "C" {
+
+const char *tbsla_last_error(void) { return g_err.c_str(); }
+
+const char *tbsla_status_string(tbsla_status_t s) {
+  switch (s) {
+  case TBSLA_OK: return "ok";
+  case TBSLA_ERR_INVALID_ARG: return "invalid argument";
+  case TBSLA_ERR_CUDA: return "CUDA error";
+  case TBSLA_ERR_OOM: return "out of device memory";
+  case TBSLA_ERR_NOT_CONVERGED: return "not converged";
+  case TBSLA_ERR_TIMEOUT: return "timeout";
+  case TBSLA_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+int tbsla_version(void) { return 100; }
+
+tbsla_status_t tbsla_set_device(int device) {
+  int n = 0;
+  TB_CUDA(cudaGetDeviceCount(&n));
+  TB_CHECK(device >= 0 && device < n, "device %d out of range (%d devices)", device, n);
+  g_device = device;
+  TB_CUDA(cudaSetDevice(device));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_csr_create(int n_row, int n_col, int f_col, int rows, const int *rowptr,
+                                const int *colidx, const double *values, int stores,
+                                tbsla_matrix_t **out) {
+  TB_CHECK(out, "out is NULL");
+  *out = nullptr;
+  TB_CHECK(n_row >= 0 && n_col >= 0 && rows >= 0 && f_col >= 0, "negative size");
+  TB_CHECK(rows <= n_row || n_row == 0, "rows %d > n_row %d", rows, n_row);
+  TB_CHECK(rowptr || rows == 0, "rowptr is NULL");
+  tbsla_matrix *A = new_handle(TBSLA_FMT_CSR);
+  if (!A) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  A->n_row = n_row; A->n_col = n_col; A->f_col = f_col; A->rows = std::min(rows, n_row);
+  static const int zero = 0;
+  const tbsla_status_t s = build_csr(A, rows ? rowptr : &zero, colidx, values, stores);
+  if (s != TBSLA_OK) { free_handle(A); return s; }
+  *out = A;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_ell_create(int n_row, int n_col, int f_col, int rows, int max_col,
+                                const int *columns, const double *values, int stores,
+                                tbsla_matrix_t **out) {
+  TB_CHECK(out, "out is NULL");
+  *out = nullptr;
+  TB_CHECK(n_row >= 0 && n_col >= 0 && rows >= 0 && max_col >= 0 && f_col >= 0, "negative size");
+  rows = std::min(rows, n_row);
+  const int64_t slots = (int64_t)rows * max_col;
+  TB_CHECK(slots == 0 || (columns && values), "NULL arrays");
+  int cmax = slots > 0 ? 0 : -1;  // padding reads x[0]
+  for (int64_t k = 0; k < slots; ++k) {
+    int c = columns[k] - f_col;
+    if (c < 0) c = 0;  // the reference's clamp (MatrixELL.cpp:108-109)
+    if (c >= n_col)
+      return fail(TBSLA_ERR_INVALID_ARG, "columns[%lld]=%d outside the column block", (long long)k, columns[k]);
+    cmax = std::max(cmax, c);
+  }
+  tbsla_matrix *A = new_handle(TBSLA_FMT_ELL);
+  if (!A) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  A->n_row = n_row; A->n_col = n_col; A->f_col = f_col; A->rows = rows; A->max_col = max_col;
+  A->rows_pad = (rows + 3) / 4 * 4;
+  A->x_extent = cmax + 1;
+  A->stored = slots;
+  // transpose to slot-major with rows padded to a multiple of four
+  const int64_t padded = (int64_t)A->rows_pad * max_col;
+  std::vector<int> cm((size_t)std::max<int64_t>(padded, 1), f_col);
+  std::vector<double> vm((size_t)std::max<int64_t>(padded, 1), 0.0);
+  for (int i = 0; i < rows; ++i)
+    for (int s = 0; s < max_col; ++s) {
+      cm[(size_t)s * A->rows_pad + i] = columns[(int64_t)i * max_col + s];
+      vm[(size_t)s * A->rows_pad + i] = values[(int64_t)i * max_col + s];
+    }
+  tbsla_status_t st = alloc_n(A, &A->idx0, padded);
+  if (st == TBSLA_OK && padded)
+    if (cudaMemcpy(A->idx0, cm.data(), padded * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+      st = fail(TBSLA_ERR_CUDA, "upload failed");
+  if (st == TBSLA_OK) st = upload_values(A, vm.data(), padded, stores);
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "sync failed");
+  if (st != TBSLA_OK) { free_handle(A); return st; }
+  *out = A;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_coo_create(int n_row, int n_col, int f_row, int f_col, int64_t nnz,
+                                const int *row, const int *col, const double *values, int stores,
+                                tbsla_matrix_t **out) {
+  TB_CHECK(out, "out is NULL");
+  *out = nullptr;
+  TB_CHECK(n_row >= 0 && n_col >= 0 && nnz >= 0 && f_row >= 0 && f_col >= 0, "negative size");
+  TB_CHECK(nnz == 0 || (row && col && values), "NULL arrays");
+  TB_CHECK(nnz <= INT_MAX, "nnz %lld exceeds the 32-bit index range", (long long)nnz);
+  // stable counting sort by row so that each row is a contiguous run in
+  // input order
+  std::vector<int64_t> cnt((size_t)n_row + 1, 0);
+  int cmax = -1;
+  for (int64_t k = 0; k < nnz; ++k) {
+    const int r = row[k] - f_row, c = col[k] - f_col;
+    if (r < 0 || r >= n_row) return fail(TBSLA_ERR_INVALID_ARG, "row[%lld]=%d outside the row block", (long long)k, row[k]);
+    if (c < 0 || c >= n_col) return fail(TBSLA_ERR_INVALID_ARG, "col[%lld]=%d outside the column block", (long long)k, col[k]);
+    cnt[r + 1]++;
+    cmax = std::max(cmax, c);
+  }
+  for (int i = 0; i < n_row; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> sr((size_t)std::max<int64_t>(nnz, 1)), sc((size_t)std::max<int64_t>(nnz, 1));
+  std::vector<double> sv((size_t)std::max<int64_t>(nnz, 1));
+  for (int64_t k = 0; k < nnz; ++k) {
+    const int64_t p = cnt[row[k] - f_row]++;
+    sr[p] = row[k] - f_row;  // stored relative to f_row
+    sc[p] = col[k];
+    sv[p] = values[k];
+  }
+  tbsla_matrix *A = new_handle(f_row == 0 && f_col == 0 ? TBSLA_FMT_COO : TBSLA_FMT_SCOO);
+  if (!A) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  A->n_row = n_row; A->n_col = n_col; A->f_row = f_row; A->f_col = f_col;
+  A->rows = n_row; A->stored = nnz; A->x_extent = cmax + 1;
+  A->num_tiles = (int)((nnz + kMergeTile - 1) / kMergeTile);
+  tbsla_status_t st = alloc_n(A, &A->idx0, nnz);
+  if (st == TBSLA_OK) st = alloc_n(A, &A->idx1, nnz);
+  if (st == TBSLA_OK && nnz) {
+    if (cudaMemcpy(A->idx0, sr.data(), nnz * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(A->idx1, sc.data(), nnz * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+      st = fail(TBSLA_ERR_CUDA, "upload failed");
+  }
+  if (st == TBSLA_OK) st = upload_values(A, sv.data(), nnz, stores);
+  if (st == TBSLA_OK) st = alloc_carries(A);
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "sync failed");
+  if (st != TBSLA_OK) { free_handle(A); return st; }
+  // COO rows are stored relative to f_row: output row = row + vect_incr
+  A->f_row = 0;
+  *out = A;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_dense_create(int n_row, int n_col, int ln_row, int ln_col,
+                                  const double *values, int stores, tbsla_matrix_t **out) {
+  TB_CHECK(out, "out is NULL");
+  *out = nullptr;
+  TB_CHECK(n_row >= 0 && n_col >= 0 && ln_row >= 0 && ln_col >= 0, "negative size");
+  const int64_t n = (int64_t)ln_row * ln_col;
+  TB_CHECK(n == 0 || values, "values is NULL");
+  tbsla_matrix *A = new_handle(TBSLA_FMT_DENSE);
+  if (!A) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  A->n_row = n_row; A->n_col = n_col; A->rows = std::min(ln_row, n_row); A->cols = ln_col;
+  A->stored = n;
+  A->x_extent = A->rows > 0 ? ln_col : 0;
+  tbsla_status_t st = upload_values(A, values, n, stores);
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "sync failed");
+  if (st != TBSLA_OK) { free_handle(A); return st; }
+  *out = A;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A) {
+  free_handle(A);
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info) {
+  TB_CHECK(A && info, "NULL argument");
+  info->format = A->format;
+  info->n_row = A->n_row; info->n_col = A->n_col;
+  info->f_row = A->f_row; info->f_col = A->f_col;
+  info->rows = A->rows; info->max_col = A->max_col;
+  info->stored = A->stored; info->stores = A->stores;
+  info->device_bytes = A->device_bytes;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_spmv(const tbsla_matrix_t *A, const double *d_x, double *d_y, int vect_incr,
+                          void *stream) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(d_y || A->n_row == 0, "y is NULL");
+  return spmv_dispatch(A, TBSLA_F64, TBSLA_F64, d_x, TBSLA_F64, d_y, vect_incr, (cudaStream_t)stream);
+}
+
+tbsla_status_t tbsla_spmv_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_dtype_t x_type,
+                             const void *d_x, tbsla_dtype_t y_type, void *d_y, int vect_incr,
+                             void *stream) {
+  TB_CHECK(A, "matrix is NULL");
+  return spmv_dispatch(A, store, x_type, d_x, y_type, d_y, vect_incr, (cudaStream_t)stream);
+}
+
+tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *y,
+                               int64_t ny, int vect_incr) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(ny >= A->n_row, "y has %lld entries, n_row is %d", (long long)ny, A->n_row);
+  TB_CHECK(nx >= A->x_extent, "x has %lld entries, the matrix reads %lld", (long long)nx, (long long)A->x_extent);
+  TB_CHECK(nx == 0 || x, "x is NULL");
+  std::lock_guard<std::mutex> lk(A->host_mu);
+  TB_CUDA(cudaSetDevice(A->device));
+  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), std::max<int64_t>(ny, 1), 0));
+  if (nx) TB_CUDA(cudaMemcpyAsync(A->d_x, x, nx * sizeof(double), cudaMemcpyHostToDevice, A->stream));
+  TB_TRY(spmv_dispatch(A, TBSLA_F64, TBSLA_F64, A->d_x, TBSLA_F64, A->d_y, vect_incr, A->stream));
+  if (A->n_row) TB_CUDA(cudaMemcpyAsync(y, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
+  TB_CUDA(cudaStreamSynchronize(A->stream));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_a_axpx(const tbsla_matrix_t *A, const double *d_x, double *d_r,
+                            double *d_tmp, int vect_incr, void *stream) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(A->n_row == A->n_col, "a_axpx needs a square matrix (%d x %d)", A->n_row, A->n_col);
+  TB_CHECK(d_tmp, "d_tmp is NULL (device pointer form needs caller scratch)");
+  return a_axpx_dispatch(A, d_x, d_r, d_tmp, vect_incr, (cudaStream_t)stream);
+}
+
+tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *r,
+                                 int64_t nr, int vect_incr) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(A->n_row == A->n_col, "a_axpx needs a square matrix (%d x %d)", A->n_row, A->n_col);
+  TB_CHECK(nx >= A->n_col && nr >= A->n_row && nx >= A->x_extent, "vector too short");
+  std::lock_guard<std::mutex> lk(A->host_mu);
+  TB_CUDA(cudaSetDevice(A->device));
+  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), std::max<int64_t>(nr, 1), std::max(A->n_row, 1)));
+  if (nx) TB_CUDA(cudaMemcpyAsync(A->d_x, x, nx * sizeof(double), cudaMemcpyHostToDevice, A->stream));
+  TB_TRY(a_axpx_dispatch(A, A->d_x, A->d_y, A->d_t, vect_incr, A->stream));
+  if (A->n_row) TB_CUDA(cudaMemcpyAsync(r, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
+  TB_CUDA(cudaStreamSynchronize(A->stream));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_device_alloc(void **ptr, size_t bytes) {
+  TB_CHECK(ptr, "ptr is NULL");
+  return dev_alloc(nullptr, ptr, bytes);
+}
+tbsla_status_t tbsla_device_free(void *ptr) {
+  if (ptr) TB_CUDA(cudaFree(ptr));
+  return TBSLA_OK;
+}
+tbsla_status_t tbsla_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream) {
+  if (bytes) TB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  return TBSLA_OK;
+}
+tbsla_status_t tbsla_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream) {
+  if (bytes) TB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  return TBSLA_OK;
+}
+tbsla_status_t tbsla_stream_sync(void *stream) {
+  TB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_host_alloc(void **ptr, size_t bytes) {
+  TB_CHECK(ptr, "ptr is NULL");
+  *ptr = nullptr;
+  TB_CUDA(cudaMallocHost(ptr, bytes ? bytes : 16));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_host_free(void *ptr) {
+  if (ptr) TB_CUDA(cudaFreeHost(ptr));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_kernel_timing_enable(tbsla_matrix_t *A, int enable) {
+  TB_CHECK(A, "matrix is NULL");
+  A->timing = enable != 0;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_kernel_timing_read(tbsla_matrix_t *A, double *total_ms, int64_t *launches) {
+  TB_CHECK(A, "matrix is NULL");
+  for (auto &e : A->pending_events) {
+    TB_CUDA(cudaEventSynchronize(e.second));
+    float ms = 0;
+    TB_CUDA(cudaEventElapsedTime(&ms, e.first, e.second));
+    A->timed_ms += ms;
+    A->timed_launches += 1;
+    A->free_events.push_back(e);
+  }
+  A->pending_events.clear();
+  if (total_ms) *total_ms = A->timed_ms;
+  if (launches) *launches = A->timed_launches;
+  A->timed_ms = 0;
+  A->timed_launches = 0;
+  return TBSLA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,270 @@
+"""Parity of the CUDA SpMV / a_axpx path with the oracle, through the C ABI.
+
+Exact equality where the reference's own tests demand it (integer-valued
+products: cqmat/cdiag with x = 0..n-1, test_spmv_cqmat.cpp:53-58 and
+test_spmv_cdiag.cpp:22-26); otherwise the FP64 bound
+|y - y_oracle| <= 1e-12 * sum_j |a_ij x_j| per row (rows split across
+threads are summed in another order than the reference's sequential loop).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import assert_close
+from test_oracle import BLOCKS, FORMATS
+
+pytestmark = pytest.mark.gpu
+
+RTOL64 = 1e-12
+
+
+class Dev:
+    """A device buffer allocated through the C ABI."""
+
+    def __init__(self, capi, n, dtype=np.float64):
+        self.capi, self.n, self.dtype = capi, n, np.dtype(dtype)
+        self.p = C.c_void_p()
+        capi.check(capi.lib().tbsla_device_alloc(C.byref(self.p), max(n, 1) * self.dtype.itemsize))
+
+    @classmethod
+    def of(cls, capi, a):
+        a = np.ascontiguousarray(a)
+        d = cls(capi, a.size, a.dtype)
+        d.upload(a)
+        return d
+
+    def upload(self, a):
+        L = self.capi.lib()
+        self.capi.check(L.tbsla_memcpy_h2d(self.p, a.ctypes.data_as(C.c_void_p), a.nbytes, None))
+        self.capi.check(L.tbsla_stream_sync(None))
+
+    def get(self):
+        out = np.zeros(max(self.n, 1), self.dtype)
+        L = self.capi.lib()
+        self.capi.check(L.tbsla_stream_sync(None))
+        self.capi.check(L.tbsla_memcpy_d2h(out.ctypes.data_as(C.c_void_p), self.p, self.n * self.dtype.itemsize,
+                                           None))
+        self.capi.check(L.tbsla_stream_sync(None))
+        return out[: self.n]
+
+    @property
+    def ptr(self):
+        return self.p.value
+
+    def __del__(self):
+        try:
+            self.capi.lib().tbsla_device_free(self.p)
+        except Exception:
+            pass
+
+
+def oracle_of(orc, g):
+    """The oracle matrix holding the same arrays as a generated one."""
+    return orc.from_layout(g.fmt, g.geom, g.nnz, g.values, g.idx0, g.idx1)
+
+
+def scale_of(orc, g, x):
+    """sum_j |a_ij x_j| with the oracle (values and x in absolute value)."""
+    from copy import copy
+    ga = copy(g)
+    ga.values = np.abs(g.values)
+    return oracle_of(orc, ga).spmv(np.abs(x))
+
+
+def gpu_spmv(capi, g, x, vect_incr=0):
+    m = capi.DeviceMatrix.from_generated(g)
+    return m.spmv_host(x, vect_incr)
+
+
+def test_known_answer(gpu, golden):
+    ka = golden["known_answer"]
+    csr = gpu.DeviceMatrix.csr(5, 5, ka["rowptr"], ka["col"], ka["values"])
+    coo = gpu.DeviceMatrix.coo(5, 5, ka["row"], ka["col"], ka["values"])
+    assert csr.spmv_host(np.array(ka["x"])).tolist() == [20, 12, 10, 40, 85]
+    assert coo.spmv_host(np.array(ka["x"])).tolist() == [20, 12, 10, 40, 85]
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_reference_sweep_exact(gpu, orc, fmt):
+    """Every format on the reference test shapes, x = 0..n-1: exact."""
+    shapes = [(10, 5, 8), (5, 10, 7), (10, 10, 12), (10, 10, 3), (10, 5, 3), (10, 5, 6)]
+    shapes += [(10, 10, i) for i in range(13)] + [(30, 30, 2 * i) for i in range(13)]
+    shapes += [(20, 30, 2 * i) for i in range(0, 13, 3)] + [(30, 20, 2 * i) for i in range(0, 13, 3)]
+    for (nr, nc, c) in shapes:
+        x = np.arange(nc, dtype=np.float64)
+        for s in (0, 1):
+            for q in (0.0, 0.1, 0.5, 1.0):
+                for blk in BLOCKS:
+                    g = gpu.generate(fmt, "cqmat", nr, nc, c, q, s, *blk)
+                    yo = oracle_of(orc, g).spmv(x)
+                    y = gpu_spmv(gpu, g, x)
+                    assert np.array_equal(y, yo), (fmt, nr, nc, c, q, s, blk, y, yo)
+        for cd in range(0, 13, 2):
+            g = gpu.generate(fmt, "cdiag", nr, nc, cd, 0.0, 0)
+            y = gpu_spmv(gpu, g, x)
+            assert np.array_equal(y, oracle_of(orc, g).spmv(x)), (fmt, "cdiag", nr, nc, cd)
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_random_x(gpu, orc, fmt):
+    rng = np.random.default_rng(11)
+    for (nr, nc, c) in [(30, 30, 6), (300, 250, 17), (1000, 1000, 40), (257, 999, 3)]:
+        for gen in ("cqmat", "cqmat_stochastic"):
+            g = gpu.generate(fmt, gen, nr, nc, c, 0.3, 2)
+            x = rng.uniform(-1, 1, nc)
+            assert_close(gpu_spmv(gpu, g, x), oracle_of(orc, g).spmv(x), scale_of(orc, g, x), RTOL64,
+                         f"{fmt} {gen} {nr}x{nc}")
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_cfg1_all_formats(gpu, orc, fmt):
+    """n=100000, c=10, q=0.1, seed 0 (the CPU-runnable headline case)."""
+    g = gpu.generate(fmt, "cqmat", 100000, 100000, 10, 0.1, 0) if fmt != "DENSE" else \
+        gpu.generate(fmt, "cqmat", 3000, 3000, 10, 0.1, 0)
+    x = np.random.default_rng(0).random(g.n_col)
+    o = oracle_of(orc, g)
+    assert_close(gpu_spmv(gpu, g, x), o.spmv(x), scale_of(orc, g, x), RTOL64, fmt)
+    if g.n_row == g.n_col:
+        m = gpu.DeviceMatrix.from_generated(g)
+        xa = np.abs(x)
+        scale = scale_of(orc, g, scale_of(orc, g, xa) + xa)
+        assert_close(m.a_axpx_host(x), o.a_axpx(x), scale, 1e-12, f"{fmt} a_axpx")
+
+
+def random_csr(rng, n_row, n_col, lengths):
+    rowptr = np.zeros(n_row + 1, np.int64)
+    rowptr[1:] = np.cumsum(lengths)
+    nnz = int(rowptr[-1])
+    colidx = rng.integers(0, n_col, nnz).astype(np.int32)
+    values = rng.standard_normal(nnz)
+    return rowptr.astype(np.int32), colidx, values
+
+
+def test_csr_skewed_rows_and_tile_edges(gpu, orc):
+    """Rows much longer than a tile, empty rows, and sizes around tile
+    boundaries (rows + nnz = k * 2304 +- 1) exercise the carry paths."""
+    rng = np.random.default_rng(3)
+    cases = []
+    lengths = rng.zipf(1.6, 5000).clip(0, 60000)
+    lengths[:7] = 0
+    lengths[-5:] = 0
+    lengths[100] = 50000
+    cases.append((5000, 7000, lengths))
+    for total in (2303, 2304, 2305, 4607, 4608, 4609, 9216 * 3 + 1):
+        n = 300
+        base = rng.integers(0, 15, n)
+        base[-1] = max(total - n - int(base[:-1].sum()), 0)
+        cases.append((n, 500, base))
+    cases.append((1, 10, np.array([0])))
+    cases.append((3, 10, np.array([0, 0, 0])))
+    cases.append((1, 100000, np.array([99999])))
+    for (nr, nc, lens) in cases:
+        rp, ci, va = random_csr(rng, nr, nc, lens)
+        x = rng.uniform(-1, 1, nc)
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va)
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+        assert_close(m.spmv_host(x), o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"csr {nr}x{nc} nnz={ci.size}")
+
+
+def test_coo_unsorted_duplicates_and_shift(gpu, orc):
+    rng = np.random.default_rng(4)
+    for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
+        row = rng.integers(0, nr, nnz).astype(np.int32)
+        col = rng.integers(0, nc, nnz).astype(np.int32)
+        val = rng.standard_normal(nnz)
+        x = rng.uniform(-1, 1, nc)
+        m = gpu.DeviceMatrix.coo(nr, nc, row, col, val)
+        o = orc.from_arrays("COO", nr, nc, val, row, col)
+        so = orc.from_arrays("COO", nr, nc, np.abs(val), row, col)
+        assert_close(m.spmv_host(x), o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"coo {nr}x{nc}")
+    # vect_incr shifts output rows (MatrixCOO.cpp:114)
+    row = np.array([0, 1, 2, 2], np.int32)
+    col = np.array([0, 1, 0, 2], np.int32)
+    val = np.array([1.0, 2.0, 3.0, 4.0])
+    m = gpu.DeviceMatrix.coo(4, 3, row, col, val)
+    assert m.spmv_host(np.array([1.0, 1.0, 1.0]), vect_incr=1).tolist() == [0, 1, 2, 7]
+
+
+def test_scoo_block_offsets(gpu, orc):
+    """SCOO/CSR/ELL/DENSE blocks of a 2x3 grid: x indexed from f_col, y from f_row."""
+    for fmt in ("SCOO", "CSR", "ELL", "DENSE"):
+        for blk in [(1, 2, 2, 3), (0, 1, 2, 3), (1, 0, 2, 3)]:
+            g = gpu.generate(fmt, "cqmat", 40, 45, 7, 0.2, 1, *blk)
+            x = np.arange(g.ln_col, dtype=np.float64) + 1
+            yo = oracle_of(orc, g).spmv(x)
+            assert np.array_equal(gpu_spmv(gpu, g, x), yo), (fmt, blk)
+
+
+def test_device_pointer_entry_points(gpu, orc):
+    g = gpu.generate("CSR", "cqmat", 5000, 5000, 12, 0.1, 0)
+    x = np.random.default_rng(9).uniform(-1, 1, 5000)
+    m = gpu.DeviceMatrix.from_generated(g)
+    dx, dy, dt = Dev.of(gpu, x), Dev(gpu, 5000), Dev(gpu, 5000)
+    m.spmv(dx.ptr, dy.ptr)
+    o = oracle_of(orc, g)
+    assert_close(dy.get(), o.spmv(x), scale_of(orc, g, x), RTOL64, "device spmv")
+    m.a_axpx(dx.ptr, dy.ptr, dt.ptr)
+    xa = np.abs(x)
+    assert_close(dy.get(), o.a_axpx(x), scale_of(orc, g, scale_of(orc, g, xa) + xa), RTOL64, "device a_axpx")
+
+
+@pytest.mark.parametrize("fmt", ["CSR", "ELL", "COO", "DENSE"])
+def test_reduced_precision_stores(gpu, orc, fmt):
+    """F32 / BF16 value stores with FP32 accumulation against the FP64 oracle:
+    |y - y64| <= rtol * sum|a x| with rtol 2e-6 (F32) and 8e-3 (BF16)."""
+    n = 20000 if fmt != "DENSE" else 1500
+    g = gpu.generate(fmt, "cqmat_stochastic", n, n, 16, 0.1, 0)
+    m = gpu.DeviceMatrix.from_generated(g, stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
+    x = np.random.default_rng(2).random(n)
+    yo = oracle_of(orc, g).spmv(x)
+    sc = scale_of(orc, g, x)
+    x32 = Dev.of(gpu, x.astype(np.float32))
+    for store, rtol in ((gpu.F32, 2e-6), (gpu.BF16, 8e-3)):
+        y32 = Dev(gpu, n, np.float32)
+        m.spmv_ex(store, gpu.F32, x32.ptr, gpu.F32, y32.ptr)
+        assert_close(y32.get().astype(np.float64), yo, sc, rtol, f"{fmt} store {store} f32 vectors")
+        y64 = Dev(gpu, n)
+        x64 = Dev.of(gpu, x)
+        m.spmv_ex(store, gpu.F64, x64.ptr, gpu.F64, y64.ptr)
+        assert_close(y64.get(), yo, sc, rtol, f"{fmt} store {store} f64 vectors")
+
+
+def test_full_size_cqmat_exact_integers(gpu):
+    """n = 2^24, c = 16, q = 0.1: with x_j = j mod 7 every product is a small
+    integer, so y must equal the row sums computed exactly on the host."""
+    n = 1 << 24
+    g = gpu.generate("CSR", "cqmat", n, n, 16, 0.1, 0)
+    x = (np.arange(n) % 7).astype(np.float64)
+    m = gpu.DeviceMatrix.from_generated(g)
+    y = m.spmv_host(x)
+    gathered = x[g.idx1]
+    expect = np.add.reduceat(gathered, g.idx0[:-1]) if gathered.size else np.zeros(n)
+    expect[np.diff(g.idx0) == 0] = 0
+    assert np.array_equal(y, expect)
+    assert y.sum() == gathered.sum()
+
+
+def test_full_size_cdiag(gpu):
+    """cdiag n = 2^26, c = 1 (the bandwidth sanity case): y_i = x_{i-1} + x_{i+1}."""
+    n = 1 << 26
+    m = gpu.DeviceMatrix.generate("CSR", "cdiag", n, n, 1)
+    x = (np.arange(n) % 1000).astype(np.float64)
+    y = m.spmv_host(x)
+    expect = np.zeros(n)
+    expect[1:] += x[:-1]
+    expect[:-1] += x[1:]
+    assert np.array_equal(y, expect)
+
+
+def test_invalid_arguments_are_reported(gpu):
+    with pytest.raises(gpu.TbslaError):
+        gpu.DeviceMatrix.csr(3, 3, [0, 2, 1, 3], [0, 1, 2], [1.0, 1.0, 1.0])  # rowptr not monotone
+    with pytest.raises(gpu.TbslaError):
+        gpu.DeviceMatrix.csr(3, 3, [0, 1, 2, 3], [0, 1, 5], [1.0, 1.0, 1.0])  # column out of range
+    with pytest.raises(gpu.TbslaError):
+        gpu.DeviceMatrix.coo(3, 3, [0, 3], [0, 0], [1.0, 1.0])  # row out of range
+    m = gpu.DeviceMatrix.csr(3, 3, [0, 1, 2, 3], [0, 1, 2], [1.0, 1.0, 1.0])
+    with pytest.raises(gpu.TbslaError):
+        m.spmv_ex(gpu.F32, gpu.F64, 0, gpu.F64, 0)  # no F32 store
