@@ -116,6 +116,10 @@ tbsla_status_t tbsla_dense_create(int n_row, int n_col, int ln_row, int ln_col,
                                   const double *values, int stores, tbsla_matrix_t **out);
 
 tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A);
+/* Kernel choice for a format with several (CSR: 0 = direct row bins, the
+ * default; 1 = shared-memory row blocks).  Results agree within the FP64
+ * bound of the parity tests; the choice only changes speed. */
+tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
 
 /* --------------------------------------------------------------- SpMV */

@@ -74,6 +74,7 @@ def lib() -> C.CDLL:
                               C.POINTER(P)], st),
         "tbsla_dense_create": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.POINTER(P)], st),
         "tbsla_matrix_destroy": ([P], st),
+        "tbsla_matrix_set_variant": ([P, C.c_int], st),
         "tbsla_matrix_info": ([P, C.POINTER(MatrixInfo)], st),
         "tbsla_spmv": ([P, _vp, _vp, C.c_int, _vp], st),
         "tbsla_spmv_ex": ([P, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp], st),
@@ -316,6 +317,9 @@ class DeviceMatrix:
         check(lib().tbsla_personalized_pagerank_host(self.h, C.byref(p), _ptr(nd), nd.size, _ptr(out),
                                                      out.size, C.byref(r)))
         return out[:n], r
+
+    def set_variant(self, variant: int):
+        check(lib().tbsla_matrix_set_variant(self.h, variant))
 
     def timing(self, enable: bool = True):
         check(lib().tbsla_kernel_timing_enable(self.h, int(enable)))

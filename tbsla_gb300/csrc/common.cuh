@@ -67,7 +67,7 @@ struct tbsla_matrix {
 
   // values in up to three precisions (F64, F32, BF16), same positions
   void *values[3] = {nullptr, nullptr, nullptr};
-  // CSR: row_end (rows ints, base removed); ELL: column-major columns
+  // CSR: rowptr (rows+1 ints, base removed); ELL: column-major columns
   // (rows_pad * max_col); COO: row (stored)
   int *idx0 = nullptr;
   // CSR: colidx; COO: col
@@ -75,15 +75,37 @@ struct tbsla_matrix {
   int rows_pad = 0;      // ELL: padded row count of the column-major arrays
   int64_t x_extent = 0;  // entries of x the kernels read (max column - f_col + 1)
 
-  // merge-path schedule (CSR, COO): tile start coordinates and carries
+  // CSR kernel variant: 0 = direct (row bins), 1 = row blocks
+  int csr_variant = 0;
+  // CSR direct bins (csr_direct.cuh): short rows (NULL = all rows), warp
+  // items (long rows and chunks of huge rows), huge rows, chunk partials
+  int *short_rows = nullptr;
+  int n_short = 0;
+  int4 *warp_items = nullptr;
+  int n_warp_items = 0;
+  int2 *chunk_rows = nullptr;
+  int n_chunk_rows = 0;
+  double *chunk_partials = nullptr;
+  float *chunk_partials32 = nullptr;
+
+  // CSR row blocks (csr_rows_kernel): descriptors, huge rows, chunk partials
+  int num_blocks = 0;
+  int4 *row_blocks = nullptr;
+  int num_huge = 0;
+  int2 *huge_rows = nullptr;         // (row, first partial slot), num_huge + 1
+  double *huge_partials = nullptr;
+  float *huge_partials32 = nullptr;
+
+  // merge-path tiles (COO): tile count and carries
   int num_tiles = 0;
-  int2 *tile_start = nullptr;   // CSR: (row, nnz) at each tile start, num_tiles+1
+  int2 *tile_start = nullptr;
   int *tile_head_row = nullptr; // per tile: row continued from an earlier tile, or -1
   double *tile_head_val = nullptr;
   double *tile_tail_val = nullptr;
   unsigned char *tile_emitted = nullptr;
   float *tile_head_val32 = nullptr;  // FP32-accumulating variants
   float *tile_tail_val32 = nullptr;
+  int *d_err = nullptr;              // set by a kernel whose bounded wait gave up
 
   // PageRank helpers built on first use
   unsigned char *dangling = nullptr;  // columns without stored entries
@@ -142,6 +164,49 @@ template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { retur
 template <> __device__ __forceinline__ __nv_bfloat16 ld_stream(const __nv_bfloat16 *p) {
   unsigned short u = __ldcs(reinterpret_cast<const unsigned short *>(p));
   return __ushort_as_bfloat16(u);
+}
+
+// L2 cache policies (createpolicy): evict-last for the gathered vector
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_normal() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// asynchronous 4/8-byte copies global -> shared (cp.async), with an L2 policy
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, uint64_t pol, int bytes) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+  if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(d), "l"(gmem), "l"(pol)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;" ::"r"(d), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <typename T> __device__ __forceinline__ T ld_keep(const T *p, uint64_t pol);
+template <> __device__ __forceinline__ double ld_keep<double>(const double *p, uint64_t pol) {
+  double v;
+  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <> __device__ __forceinline__ float ld_keep<float>(const float *p, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
 }
 
 // gathered vector loads (read-only path)

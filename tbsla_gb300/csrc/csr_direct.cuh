@@ -1,0 +1,196 @@
+// csr_direct.cuh -- direct CSR SpMV kernels for sm_103a (the default CSR path).
+//
+// Rows are binned at creation by length:
+//   short (<= kShortRow nonzeros): one thread per row, walking its row in
+//     chunks of eight entries with 16-byte loads straight from global memory.
+//     Lanes of a warp hold neighbouring rows; the loads of one chunk are
+//     issued together, so a sector's second use hits the line already in
+//     flight in L1: L1 does the coalescing, no shared memory and no block
+//     barrier are involved.  The row is summed in
+//     its stored order with one FMA per nonzero (the order of
+//     MatrixCSR::Ax, src/cpp/matrix/MatrixCSR.cpp:133-139).
+//   long (<= kChunk): one warp per row, lanes striding the row, partial sums
+//     combined with a fixed shuffle tree.
+//   huge (> kChunk): the row is cut into chunks of kChunk nonzeros, one warp
+//     per chunk writing a partial; csr_chunk_fixup_kernel adds the partials of
+//     each row in chunk order.
+// Row data is read through L1 with the default cache policy, the gathered x
+// evict-last in L2, y written with streaming stores.  No atomics: results do not depend on scheduling.
+#pragma once
+
+#include <type_traits>
+
+#include "spmv_kernels.cuh"
+
+namespace tbsla {
+
+constexpr int kShortRow = 32;
+constexpr int kChunk = 8192;
+
+__device__ __forceinline__ float bf16_lo(unsigned w) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w & 0xffffu))); }
+__device__ __forceinline__ float bf16_hi(unsigned w) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w >> 16))); }
+
+// eight entries from an 8-aligned index with 16-byte loads through L1 and the
+// default cache policy (arrays carry 64 bytes of padding, so a group may run
+// past the last entry).  A lane reads each sector in two pieces; L1/L2 keep
+// the line between them.  Explicit L2 hints were measured worse here: an
+// evict-first hint lets L2 drop the line between the two reads (DRAM traffic
+// x2.5), and 32-byte loads with an evict-normal policy ran 20% slower.
+__device__ __forceinline__ void ld_vals8(const double *p, double (&v)[8]) {
+  #pragma unroll
+  for (int h = 0; h < 4; ++h) {
+    const double2 d = __ldg(reinterpret_cast<const double2 *>(p) + h);
+    v[2 * h] = d.x; v[2 * h + 1] = d.y;
+  }
+}
+__device__ __forceinline__ void ld_vals8(const float *p, float (&v)[8]) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void ld_vals8(const __nv_bfloat16 *p, float (&v)[8]) {
+  const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+  #pragma unroll
+  for (int h = 0; h < 4; ++h) { v[2 * h] = bf16_lo(w[h]); v[2 * h + 1] = bf16_hi(w[h]); }
+}
+__device__ __forceinline__ void ld_cols8(const int *c, int (&col)[8]) {
+  const int4 a = __ldg(reinterpret_cast<const int4 *>(c));
+  const int4 b = __ldg(reinterpret_cast<const int4 *>(c) + 1);
+  col[0] = a.x; col[1] = a.y; col[2] = a.z; col[3] = a.w;
+  col[4] = b.x; col[5] = b.y; col[6] = b.z; col[7] = b.w;
+}
+// two entries from an even index
+__device__ __forceinline__ void ld_vals2(const double *p, double (&v)[2]) {
+  const double2 d = __ldg(reinterpret_cast<const double2 *>(p));
+  v[0] = d.x; v[1] = d.y;
+}
+__device__ __forceinline__ void ld_vals2(const float *p, float (&v)[2]) {
+  const float2 d = __ldg(reinterpret_cast<const float2 *>(p));
+  v[0] = d.x; v[1] = d.y;
+}
+__device__ __forceinline__ void ld_vals2(const __nv_bfloat16 *p, float (&v)[2]) {
+  const unsigned w = __ldg(reinterpret_cast<const unsigned *>(p));
+  v[0] = bf16_lo(w); v[1] = bf16_hi(w);
+}
+
+// One row, one thread.  Rows of eight or more entries go in groups of eight
+// aligned to eight, all loads of a group issued together; shorter rows go in
+// aligned pairs, which neighbouring lanes read as contiguous 16-byte pieces.
+// Entries outside [a, b) of a group are masked (no gather, no FMA).  The row
+// is summed in stored order, one FMA per entry.
+template <int G, typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc row_groups(const int *__restrict__ colidx, const V *__restrict__ values,
+                                          const XT *__restrict__ x, int f_col, int a, int b, uint64_t keep) {
+  using Ld = typename std::conditional<sizeof(V) == 8, double, float>::type;
+  Acc acc = 0;
+  for (int base = a & ~(G - 1); base < b; base += G) {
+    Ld v[G];
+    int col[G];
+    if constexpr (G == 2) {
+      ld_vals2(values + base, v);
+      const int2 c = __ldg(reinterpret_cast<const int2 *>(colidx + base));
+      col[0] = c.x; col[1] = c.y;
+    } else {
+      ld_vals8(values + base, v);
+      ld_cols8(colidx + base, col);
+    }
+    Acc xv[G];
+    #pragma unroll
+    for (int e = 0; e < G; ++e) {
+      const int k = base + e;
+      xv[e] = (k >= a && k < b) ? to_acc(ld_keep(x + (col[e] - f_col), keep), Acc()) : Acc(0);
+    }
+    #pragma unroll
+    for (int e = 0; e < G; ++e) {
+      const int k = base + e;
+      if (k >= a && k < b) acc = fma_acc((Acc)v[e], xv[e], acc);
+    }
+  }
+  return acc;
+}
+
+template <typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc row_sum_thread(const int *__restrict__ colidx, const V *__restrict__ values,
+                                              const XT *__restrict__ x, int f_col, int a, int b,
+                                              uint64_t keep) {
+  if (b - a >= 8) return row_groups<8, V, XT, Acc>(colidx, values, x, f_col, a, b, keep);
+  return row_groups<2, V, XT, Acc>(colidx, values, x, f_col, a, b, keep);
+}
+
+// short rows: rows [0, n_rows) when `rows` is NULL, else rows[0..n_rows)
+template <typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ rows, int n_rows,
+                                                       const int *__restrict__ rowptr,
+                                                       const int *__restrict__ colidx,
+                                                       const V *__restrict__ values,
+                                                       const XT *__restrict__ x, int f_col, Epi epi) {
+  using Acc = typename Epi::Acc;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  typename Epi::State es{};
+  if (t < n_rows) {
+    const int r = rows ? __ldg(rows + t) : t;
+    const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
+    const uint64_t keep = policy_evict_last();
+    epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
+// sum of entries [a, b) by one warp: lanes stride the range, fixed shuffle tree
+template <typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc range_sum_warp(const int *__restrict__ colidx, const V *__restrict__ values,
+                                              const XT *__restrict__ x, int f_col, int a, int b,
+                                              uint64_t keep) {
+  const int lane = threadIdx.x & 31;
+  Acc acc = 0;
+  #pragma unroll 4
+  for (int k = a + lane; k < b; k += 32)
+    acc = fma_acc(to_acc(ld_stream(values + k), Acc()), to_acc(ld_keep(x + (ld_stream(colidx + k) - f_col), keep), Acc()), acc);
+  #pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  return acc;  // valid in lane 0
+}
+
+// long rows (one warp each) and chunks of huge rows (one warp each):
+// items[w] = (row, begin, end, partial slot or -1)
+template <typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_warp_kernel(const int4 *__restrict__ items, int n_items,
+                                                      const int *__restrict__ colidx,
+                                                      const V *__restrict__ values,
+                                                      const XT *__restrict__ x, int f_col,
+                                                      typename Epi::Acc *__restrict__ partials, Epi epi) {
+  using Acc = typename Epi::Acc;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  typename Epi::State es{};
+  if (w < n_items) {
+    const int4 it = items[w];
+    const uint64_t keep = policy_evict_last();
+    const Acc s = range_sum_warp<V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
+    if ((threadIdx.x & 31) == 0) {
+      if (it.w < 0) epi.emit(it.x, s, es);
+      else partials[it.w] = s;
+    }
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
+// y[row] = sum of the row's chunk partials in chunk order;
+// huge[h] = (row, first slot), huge[n_huge].y = total slots
+template <typename Epi>
+__global__ void csr_chunk_fixup_kernel(const int2 *__restrict__ huge, int n_huge,
+                                       const typename Epi::Acc *__restrict__ partials, Epi epi) {
+  using Acc = typename Epi::Acc;
+  const int h = blockIdx.x * blockDim.x + threadIdx.x;
+  typename Epi::State es{};
+  if (h < n_huge) {
+    const int row = huge[h].x, first = huge[h].y, last = huge[h + 1].y;
+    Acc s = partials[first];
+    for (int c = first + 1; c < last; ++c) s += partials[c];
+    epi.emit(row, s, es);
+  }
+  epi.fixup_done(es, n_huge);
+}
+
+}  // namespace tbsla

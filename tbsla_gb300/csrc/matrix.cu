@@ -8,6 +8,8 @@
 #include <vector>
 
 #include "common.cuh"
+#include "csr_direct.cuh"
+#include "csr_rows.cuh"
 #include "spmv_kernels.cuh"
 
 namespace tbsla {
@@ -41,13 +43,14 @@ int current_device() {
 tbsla_status_t dev_alloc(tbsla_matrix *A, void **p, size_t bytes) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
-  // 16 spare bytes so that vector loads of a ragged end stay inside
-  cudaError_t e = cudaMalloc(p, bytes + 16);
+  // 64 spare bytes: vector loads and 16-byte aligned bulk copies of a
+  // ragged end stay inside the allocation
+  cudaError_t e = cudaMalloc(p, bytes + 64);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(TBSLA_ERR_OOM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
   }
-  if (A) A->device_bytes += (int64_t)bytes + 16;
+  if (A) A->device_bytes += (int64_t)bytes + 64;
   return TBSLA_OK;
 }
 
@@ -139,26 +142,10 @@ static tbsla_status_t upload_values(tbsla_matrix *A, const double *host, int64_t
   } else {
     TB_CUDA(cudaDeviceSynchronize());
     cudaFree(d64);
-    A->device_bytes -= (int64_t)std::max<int64_t>(n, 1) * 8 + 16;
+    A->device_bytes -= (int64_t)std::max<int64_t>(n, 1) * 8 + 64;
   }
   A->stores = stores & (TBSLA_STORE_F64 | TBSLA_STORE_F32 | TBSLA_STORE_BF16);
   return TBSLA_OK;
-}
-
-// ------------------------------------------------- merge-path schedule
-// tile_start[t] = merge-path coordinate (row, nonzero) of diagonal t*TILE
-__global__ void csr_schedule_kernel(const int *row_end, int rows, int nnz, int num_tiles,
-                                    int2 *tile_start) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t > num_tiles) return;
-  const int64_t full = (int64_t)t * kMergeTile, end = (int64_t)rows + nnz;
-  const int d = (int)(full < end ? full : end);
-  int lo = max(d - nnz, 0), hi = min(d, rows);
-  while (lo < hi) {
-    const int p = (lo + hi) >> 1;
-    if (row_end[p] <= d - p - 1) lo = p + 1; else hi = p;
-  }
-  tile_start[t] = make_int2(lo, d - lo);
 }
 
 static tbsla_status_t alloc_carries(tbsla_matrix *A) {
@@ -169,6 +156,8 @@ static tbsla_status_t alloc_carries(tbsla_matrix *A) {
   TB_TRY(alloc_n(A, &A->tile_emitted, nt));
   TB_TRY(alloc_n(A, &A->tile_head_val32, nt));
   TB_TRY(alloc_n(A, &A->tile_tail_val32, nt));
+  TB_TRY(alloc_n(A, &A->d_err, 1));
+  TB_CUDA(cudaMemset(A->d_err, 0, sizeof(int)));
   return TBSLA_OK;
 }
 
@@ -185,9 +174,11 @@ static void free_handle(tbsla_matrix *A) {
   if (!A) return;
   cudaSetDevice(A->device);
   for (void *p : A->values) if (p) cudaFree(p);
-  void *ptrs[] = {A->idx0, A->idx1, A->tile_start, A->tile_head_row, A->tile_head_val,
+  void *ptrs[] = {A->idx0, A->idx1, A->row_blocks, A->huge_rows, A->huge_partials, A->huge_partials32,
+                  A->short_rows, A->warp_items, A->chunk_rows, A->chunk_partials, A->chunk_partials32,
+                  A->tile_start, A->tile_head_row, A->tile_head_val,
                   A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
-                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t};
+                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err};
   for (void *p : ptrs) if (p) cudaFree(p);
   if (A->stream) cudaStreamDestroy(A->stream);
   for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -206,18 +197,51 @@ template <> Carry<float> carry_of<float>(const tbsla_matrix *A) {
 }
 
 // ------------------------------------------------------------ launches
+// Dynamic shared memory of csr_rows_kernel (set once per instantiation).
+template <typename V, typename XT, typename Epi> size_t csr_rows_setup() {
+  constexpr size_t smem = csr_rows_smem<typename Epi::Acc>();
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(csr_rows_kernel<V, XT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    done = true;
+  }
+  return smem;
+}
+
+template <typename Acc> Acc *huge_partials_of(const tbsla_matrix *A);
+template <> double *huge_partials_of<double>(const tbsla_matrix *A) { return A->huge_partials; }
+template <> float *huge_partials_of<float>(const tbsla_matrix *A) { return A->huge_partials32; }
+template <typename Acc> Acc *chunk_partials_of(const tbsla_matrix *A);
+template <> double *chunk_partials_of<double>(const tbsla_matrix *A) { return A->chunk_partials; }
+template <> float *chunk_partials_of<float>(const tbsla_matrix *A) { return A->chunk_partials32; }
+
 template <typename V, typename XT, typename Epi>
 tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x, Epi epi,
                               cudaStream_t s) {
   using Acc = typename Epi::Acc;
   switch (A->format) {
   case TBSLA_FMT_CSR:
-    if (A->rows > 0) {
+    if (A->rows > 0 && A->csr_variant == 0) {
       KernelTimer kt(A, s);
-      csr_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
-          A->idx0, A->idx1, vals, x, A->f_col, A->rows, A->tile_start, carry_of<Acc>(A), epi);
+      if (A->n_short > 0)
+        csr_short_kernel<V, XT, Epi><<<(A->n_short + 255) / 256, 256, 0, s>>>(A->short_rows, A->n_short, A->idx0,
+                                                                             A->idx1, vals, x, A->f_col, epi);
+      if (A->n_warp_items > 0)
+        csr_warp_kernel<V, XT, Epi><<<(A->n_warp_items + 7) / 8, 256, 0, s>>>(
+            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, chunk_partials_of<Acc>(A), epi);
       kt.stop();
-      merge_fixup_kernel<Epi><<<(A->num_tiles + 255) / 256, 256, 0, s>>>(A->num_tiles, carry_of<Acc>(A), epi);
+      if (A->n_chunk_rows > 0)
+        csr_chunk_fixup_kernel<Epi><<<(A->n_chunk_rows + 127) / 128, 128, 0, s>>>(
+            A->chunk_rows, A->n_chunk_rows, chunk_partials_of<Acc>(A), epi);
+    } else if (A->rows > 0) {
+      const size_t smem = csr_rows_setup<V, XT, Epi>();
+      KernelTimer kt(A, s);
+      csr_rows_kernel<V, XT, Epi><<<A->num_blocks, kRowsNT, smem, s>>>(
+          A->row_blocks, A->idx0, A->idx1, vals, x, A->f_col, huge_partials_of<Acc>(A), epi);
+      kt.stop();
+      if (A->num_huge > 0)
+        csr_huge_fixup_kernel<Epi><<<(A->num_huge + 127) / 128, 128, 0, s>>>(A->huge_rows, A->num_huge,
+                                                                            huge_partials_of<Acc>(A), epi);
     }
     break;
   case TBSLA_FMT_COO:
@@ -351,21 +375,56 @@ tbsla_status_t axpy_inplace(double *y, const double *x, int64_t n, cudaStream_t 
 }
 
 // ------------------------------------------------------------ creation
+// Cuts rows [0, rows) into blocks of csr_rows_kernel: at most kRowsMax rows,
+// kRowsMax segments (of at most kSeg nonzeros) and kRowsCap nonzeros per
+// block; a row longer than kRowsCap is huge and gets one block per chunk.
+static void plan_row_blocks(const std::vector<int> &rp, std::vector<int4> &blocks,
+                            std::vector<int2> &huge, int *n_partials) {
+  const int rows = (int)rp.size() - 1;
+  int slot = 0, cur_r0 = 0, cur_rows = 0, cur_segs = 0, cur_nnz = 0;
+  auto close = [&](int r_end) {
+    if (cur_rows > 0) blocks.push_back(make_int4(cur_r0, r_end, rp[cur_r0], -1));
+    cur_rows = 0;
+    cur_segs = 0;
+    cur_nnz = 0;
+  };
+  for (int r = 0; r < rows; ++r) {
+    const int len = rp[r + 1] - rp[r];
+    const int nseg = len > kSeg ? (len + kSeg - 1) / kSeg : 1;
+    if (len > kRowsCap) {
+      close(r);
+      huge.push_back(make_int2(r, slot));
+      for (int c = 0; c < len; c += kRowsCap) blocks.push_back(make_int4(r, r + 1, rp[r] + c, slot++));
+      cur_r0 = r + 1;
+      continue;
+    }
+    if (cur_rows + 1 > kRowsMax || cur_segs + nseg > kRowsMax || cur_nnz + len > kRowsCap) {
+      close(r);
+      cur_r0 = r;
+    }
+    if (cur_rows == 0) cur_r0 = r;
+    ++cur_rows;
+    cur_segs += nseg;
+    cur_nnz += len;
+  }
+  close(rows);
+  huge.push_back(make_int2(-1, slot));
+  *n_partials = slot;
+}
+
 static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *colidx,
                                 const double *values, int stores) {
   const int rows = A->rows;
-  const int base = rows >= 0 ? rowptr[0] : 0;
+  const int base = rowptr[0];
   const int64_t nnz = (int64_t)rowptr[rows] - base;
   if (nnz < 0 || nnz > INT_MAX) return fail(TBSLA_ERR_INVALID_ARG, "bad rowptr range");
-  std::vector<int> row_end((size_t)std::max(rows, 1));
-  int prev = base;
-  for (int i = 0; i < rows; ++i) {
-    const int e = rowptr[i + 1];
-    if (e < prev) return fail(TBSLA_ERR_INVALID_ARG, "rowptr is not monotone at row %d", i);
-    row_end[i] = e - base;
-    prev = e;
-  }
   if ((int64_t)rows + nnz > INT_MAX) return fail(TBSLA_ERR_INVALID_ARG, "rows + nnz exceeds the 32-bit index range");
+  std::vector<int> rp((size_t)rows + 1);
+  rp[0] = 0;
+  for (int i = 0; i < rows; ++i) {
+    if (rowptr[i + 1] < rowptr[i]) return fail(TBSLA_ERR_INVALID_ARG, "rowptr is not monotone at row %d", i);
+    rp[i + 1] = rowptr[i + 1] - base;
+  }
   int cmax = -1;
   for (int64_t k = 0; k < nnz; ++k) {
     const int c = colidx[k] - A->f_col;
@@ -374,17 +433,56 @@ static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *c
   }
   A->x_extent = cmax + 1;
   A->stored = nnz;
-  TB_TRY(alloc_n(A, &A->idx0, rows));
+  TB_TRY(alloc_n(A, &A->idx0, (int64_t)rows + 1));
   TB_TRY(alloc_n(A, &A->idx1, nnz));
-  if (rows) TB_CUDA(cudaMemcpy(A->idx0, row_end.data(), rows * sizeof(int), cudaMemcpyHostToDevice));
+  TB_CUDA(cudaMemcpy(A->idx0, rp.data(), ((size_t)rows + 1) * sizeof(int), cudaMemcpyHostToDevice));
   if (nnz) TB_CUDA(cudaMemcpy(A->idx1, colidx, nnz * sizeof(int), cudaMemcpyHostToDevice));
   TB_TRY(upload_values(A, values, nnz, stores));
-  const int64_t items = (int64_t)rows + nnz;
-  A->num_tiles = (int)((items + kMergeTile - 1) / kMergeTile);
-  TB_TRY(alloc_n(A, &A->tile_start, A->num_tiles + 1));
-  csr_schedule_kernel<<<(A->num_tiles + 1 + 255) / 256, 256>>>(A->idx0, rows, (int)nnz, A->num_tiles, A->tile_start);
-  TB_CUDA(cudaGetLastError());
-  TB_TRY(alloc_carries(A));
+  // direct bins: short rows by thread, long rows by warp, huge rows by chunk
+  {
+    std::vector<int> shorts;
+    std::vector<int4> items;
+    std::vector<int2> chunk_rows;
+    int slot = 0;
+    bool all_short = true;
+    for (int r = 0; r < rows; ++r) {
+      const int len = rp[r + 1] - rp[r];
+      if (len <= kShortRow) { shorts.push_back(r); continue; }
+      all_short = false;
+      if (len <= kChunk) { items.push_back(make_int4(r, rp[r], rp[r + 1], -1)); continue; }
+      chunk_rows.push_back(make_int2(r, slot));
+      for (int c = rp[r]; c < rp[r + 1]; c += kChunk) items.push_back(make_int4(r, c, std::min(c + kChunk, rp[r + 1]), slot++));
+    }
+    A->n_short = (int)shorts.size();
+    if (!all_short && !shorts.empty()) {
+      TB_TRY(alloc_n(A, &A->short_rows, (int64_t)shorts.size()));
+      TB_CUDA(cudaMemcpy(A->short_rows, shorts.data(), shorts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    A->n_warp_items = (int)items.size();
+    if (!items.empty()) {
+      TB_TRY(alloc_n(A, &A->warp_items, (int64_t)items.size()));
+      TB_CUDA(cudaMemcpy(A->warp_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    }
+    A->n_chunk_rows = (int)chunk_rows.size();
+    chunk_rows.push_back(make_int2(-1, slot));
+    TB_TRY(alloc_n(A, &A->chunk_rows, (int64_t)chunk_rows.size()));
+    TB_CUDA(cudaMemcpy(A->chunk_rows, chunk_rows.data(), chunk_rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    TB_TRY(alloc_n(A, &A->chunk_partials, std::max(slot, 1)));
+    TB_TRY(alloc_n(A, &A->chunk_partials32, std::max(slot, 1)));
+  }
+  std::vector<int4> blocks;
+  std::vector<int2> huge;
+  int n_partials = 0;
+  plan_row_blocks(rp, blocks, huge, &n_partials);
+  A->num_blocks = (int)blocks.size();
+  A->num_huge = (int)huge.size() - 1;
+  TB_TRY(alloc_n(A, &A->row_blocks, std::max<int64_t>((int64_t)blocks.size(), 1)));
+  TB_TRY(alloc_n(A, &A->huge_rows, (int64_t)huge.size()));
+  TB_TRY(alloc_n(A, &A->huge_partials, std::max(n_partials, 1)));
+  TB_TRY(alloc_n(A, &A->huge_partials32, std::max(n_partials, 1)));
+  if (!blocks.empty())
+    TB_CUDA(cudaMemcpy(A->row_blocks, blocks.data(), blocks.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  TB_CUDA(cudaMemcpy(A->huge_rows, huge.data(), huge.size() * sizeof(int2), cudaMemcpyHostToDevice));
   TB_CUDA(cudaDeviceSynchronize());
   return TBSLA_OK;
 }
@@ -548,6 +646,17 @@ tbsla_status_t tbsla_dense_create(int n_row, int n_col, int ln_row, int ln_col,
   if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "sync failed");
   if (st != TBSLA_OK) { free_handle(A); return st; }
   *out = A;
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant) {
+  TB_CHECK(A, "matrix is NULL");
+  if (A->format == TBSLA_FMT_CSR) {
+    TB_CHECK(variant == 0 || variant == 1, "CSR kernel variant %d unknown (0 direct, 1 row blocks)", variant);
+    A->csr_variant = variant;
+    return TBSLA_OK;
+  }
+  TB_CHECK(variant == 0, "format %d has a single kernel", A->format);
   return TBSLA_OK;
 }
 

@@ -1,9 +1,8 @@
 // spmv_kernels.cuh -- sm_103a SpMV kernels for the five TBSLA formats.
 //
-// CSR and COO use a merge-path decomposition: every thread consumes exactly
-// kMergeItems items (a nonzero, or for CSR the end of a row) from a tile of
-// kMergeTile items staged in shared memory, accumulating its rows
-// sequentially with one FMA per nonzero.  A row that spans several threads
+// COO uses a merge-path decomposition: every thread consumes exactly
+// kMergeItems nonzeros from a tile of kMergeTile entries staged in shared
+// memory, accumulating its rows sequentially with one FMA per nonzero.  A row that spans several threads
 // is finished by the thread where it ends, which adds the partial sums of the
 // earlier threads in path order; a row that spans tiles is finished by
 // merge_fixup_kernel from the per-tile head/tail partials.  No atomics: the
@@ -38,7 +37,7 @@ template <typename YT, typename AccT> struct StoreEpi {
   int shift;   // output row = row + shift (COO vect_incr)
   __device__ __forceinline__ void emit(int row, Acc v, State &) const {
     int o = row + shift;
-    if (o >= 0 && o < n_out) y[o] = (YT)v;
+    if (o >= 0 && o < n_out) __stcs(y + o, (YT)v);  // streaming: keep L2 for x
   }
   __device__ __forceinline__ void block_done(State &, int) const {}
   __device__ __forceinline__ void fixup_done(State &, int) const {}
@@ -54,7 +53,7 @@ template <typename AccT> struct AddXEpi {
   int shift;
   __device__ __forceinline__ void emit(int row, Acc v, State &) const {
     int o = row + shift;
-    if (o >= 0 && o < n_out) y[o] = (double)v + x[o];
+    if (o >= 0 && o < n_out) __stcs(y + o, (double)v + x[o]);
   }
   __device__ __forceinline__ void block_done(State &, int) const {}
   __device__ __forceinline__ void fixup_done(State &, int) const {}
@@ -130,85 +129,30 @@ __device__ __forceinline__ void resolve_tile(int tile, bool deferred, int first_
   }
 }
 
-// --------------------------------------------------------------- CSR
-// Tile t covers merge-path diagonals [t*TILE, (t+1)*TILE); tile_start holds
-// its (row, nonzero) start coordinates (num_tiles + 1 entries).
-template <int NT, int K, typename V, typename XT, typename Epi>
-__global__ void __launch_bounds__(NT) csr_merge_kernel(const int *__restrict__ row_end,
-                                                       const int *__restrict__ colidx,
-                                                       const V *__restrict__ values,
-                                                       const XT *__restrict__ x, int f_col, int rows,
-                                                       const int2 *__restrict__ tile_start,
-                                                       Carry<typename Epi::Acc> carry, Epi epi) {
-  using Acc = typename Epi::Acc;
-  constexpr int TILE = NT * K;
-  __shared__ int s_rs[TILE + 2];
-  __shared__ V s_val[TILE];
-  __shared__ int s_col[TILE];
-  __shared__ Acc s_tail[NT];
-  __shared__ Acc s_red[NT / 32 + 1];
-  __shared__ unsigned char s_emit[NT];
-  __shared__ int s_misc[NT / 32 + 2];
-
-  const int t = blockIdx.x;
-  const int2 st = tile_start[t], en = tile_start[t + 1];
-  const int i0 = st.x, j0 = st.y, i1 = en.x, j1 = en.y;
-  const int nrow_t = i1 - i0, nnz_t = j1 - j0;
-  // s_rs[k] = end of row i0-1+k (0 for row -1): row i starts at s_rs[i-i0]
-  // and ends at s_rs[i-i0+1]
-  const int n_rs = nrow_t + 1 + (i1 < rows ? 1 : 0);
-  for (int k = threadIdx.x; k < n_rs; k += NT) {
-    const int r = i0 - 1 + k;
-    s_rs[k] = r < 0 ? 0 : row_end[r];
-  }
-  for (int k = threadIdx.x; k < nnz_t; k += NT) {
-    s_val[k] = ld_stream(values + j0 + k);
-    s_col[k] = ld_stream(colidx + j0 + k);
-  }
-  __syncthreads();
-
-  const int total = nrow_t + nnz_t;
-  const int dl = min((int)threadIdx.x * K, total);
-  int lo = max(dl - nnz_t, 0), hi = min(dl, nrow_t);
-  while (lo < hi) {
-    const int p = (lo + hi) >> 1;
-    if (s_rs[p + 1] <= j0 + dl - p - 1) lo = p + 1; else hi = p;
-  }
-  int i = i0 + lo, j = j0 + dl - lo;
-  const int n_items = min(dl + K, total) - dl;
-  const bool starts_mid = (i < rows) && (j > s_rs[i - i0]);
-  int rend = (i < rows) ? s_rs[i - i0 + 1] : INT_MAX;
-
-  typename Epi::State es{};
-  Acc acc = 0, first_val = 0;
-  bool emitted = false, deferred = false;
-  int first_row = -1;
+// Stages n (<= NT*K) consecutive nonzeros of a tile in shared memory: the
+// values, and the gathered x[col - f_col] in the accumulator type.  Thread k
+// takes nonzeros k, k+NT, ...: the index and value loads are coalesced, all K
+// gathers of a thread are in flight together, and neighbouring threads
+// gather neighbouring columns of a row (band entries are consecutive).
+template <int NT, int K, typename V, typename XT, typename Acc>
+__device__ __forceinline__ void stage_tile(const V *__restrict__ vals, const int *__restrict__ cols,
+                                           const XT *__restrict__ x, int f_col, int n, V *s_val,
+                                           Acc *s_x) {
+  const uint64_t keep = policy_evict_last();
+  int c[K];
   #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    if (k < n_items) {
-      if (j < rend) {
-        const int jj = j - j0;
-        acc = fma_acc(to_acc(s_val[jj], Acc()), to_acc(ld_vec(x + (s_col[jj] - f_col)), Acc()), acc);
-        ++j;
-      } else {
-        if (!emitted && starts_mid) {
-          deferred = true; first_row = i; first_val = acc;
-        } else {
-          epi.emit(i, acc, es);
-        }
-        emitted = true;
-        acc = 0;
-        ++i;
-        rend = (i < rows) ? s_rs[i - i0 + 1] : INT_MAX;
-      }
+  for (int u = 0; u < K; ++u) {
+    const int k = threadIdx.x + u * NT;
+    c[u] = k < n ? ld_stream(cols + k) : f_col;
+  }
+  #pragma unroll
+  for (int u = 0; u < K; ++u) {
+    const int k = threadIdx.x + u * NT;
+    if (k < n) {
+      s_val[k] = ld_stream(vals + k);
+      s_x[k] = to_acc(ld_keep(x + (c[u] - f_col), keep), Acc());
     }
   }
-  s_tail[threadIdx.x] = acc;
-  s_emit[threadIdx.x] = emitted;
-  const bool tile_starts_mid = (i0 < rows) && (j0 > s_rs[0]);
-  resolve_tile<NT, Epi>(t, deferred, first_row, first_val, tile_starts_mid, s_tail, s_emit, s_misc,
-                        s_red, carry, epi, es);
-  epi.block_done(es, t);
 }
 
 // rows that span tiles: the tile where the row ends adds the tails of the
@@ -245,7 +189,7 @@ __global__ void __launch_bounds__(NT) coo_merge_kernel(const int *__restrict__ r
   constexpr int TILE = NT * K;
   __shared__ int s_row[TILE];
   __shared__ V s_val[TILE];
-  __shared__ int s_col[TILE];
+  __shared__ Acc s_x[TILE];
   __shared__ Acc s_tail[NT];
   __shared__ Acc s_red[NT / 32 + 1];
   __shared__ unsigned char s_emit[NT];
@@ -254,11 +198,8 @@ __global__ void __launch_bounds__(NT) coo_merge_kernel(const int *__restrict__ r
   const int t = blockIdx.x;
   const int64_t e0 = (int64_t)t * TILE;
   const int n_t = (int)min((int64_t)TILE, nnz - e0);
-  for (int k = threadIdx.x; k < n_t; k += NT) {
-    s_row[k] = ld_stream(rowv + e0 + k);
-    s_val[k] = ld_stream(values + e0 + k);
-    s_col[k] = ld_stream(colv + e0 + k);
-  }
+  for (int k = threadIdx.x; k < n_t; k += NT) s_row[k] = ld_stream(rowv + e0 + k);
+  stage_tile<NT, K, V, XT, Acc>(values + e0, colv + e0, x, f_col, n_t, s_val, s_x);
   const int prev_row = e0 > 0 ? rowv[e0 - 1] : -1;
   __syncthreads();
 
@@ -277,7 +218,7 @@ __global__ void __launch_bounds__(NT) coo_merge_kernel(const int *__restrict__ r
     if (k < n_items) {
       const int e = b + k;
       const int r = s_row[e];
-      acc = fma_acc(to_acc(s_val[e], Acc()), to_acc(ld_vec(x + (s_col[e] - f_col)), Acc()), acc);
+      acc = fma_acc(to_acc(s_val[e], Acc()), s_x[e], acc);
       const int nr = (e + 1 < n_t) ? s_row[e + 1] : next_tile_row;
       if (nr != r) {  // the row ends at entry e
         if (!emitted && starts_mid) { deferred = true; first_row = r; first_val = acc; }
@@ -329,7 +270,9 @@ __global__ void __launch_bounds__(256) ell_kernel(const int *__restrict__ cols,
   const int r0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
   typename Epi::State es{};
   if (r0 < rows) {
+    const uint64_t keep = policy_evict_last();
     Acc a[4] = {0, 0, 0, 0};
+    #pragma unroll 4
     for (int s = 0; s < max_col; ++s) {
       const size_t off = (size_t)s * rows_pad + r0;
       const int4 c = __ldcs(reinterpret_cast<const int4 *>(cols + off));
@@ -339,7 +282,7 @@ __global__ void __launch_bounds__(256) ell_kernel(const int *__restrict__ cols,
       for (int q = 0; q < 4; ++q) {
         int idx = cc[q] - f_col;
         if (idx < 0) idx = 0;
-        a[q] = fma_acc(to_acc(v.v[q], Acc()), to_acc(ld_vec(x + idx), Acc()), a[q]);
+        a[q] = fma_acc(to_acc(v.v[q], Acc()), to_acc(ld_keep(x + idx, keep), Acc()), a[q]);
       }
     }
     #pragma unroll

@@ -168,6 +168,25 @@ def test_csr_skewed_rows_and_tile_edges(gpu, orc):
         assert_close(m.spmv_host(x), o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"csr {nr}x{nc} nnz={ci.size}")
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+def test_csr_kernel_variants(gpu, orc, variant):
+    """Both CSR kernels (direct row bins, shared-memory row blocks) on
+    uniform, skewed and huge-row matrices."""
+    rng = np.random.default_rng(8)
+    lens_skew = rng.zipf(1.5, 30000).clip(0, 40000)
+    lens_skew[:3] = 0
+    lens_skew[123] = 20000
+    for (nr, nc, lens) in [(20000, 20000, np.full(20000, 16)), (30000, 40000, lens_skew),
+                           (50, 300000, np.array([0, 9000, 33, 17000] + [5] * 46)), (40000, 9, np.full(40000, 2))]:
+        rp, ci, va = random_csr(rng, nr, nc, lens)
+        x = rng.uniform(-1, 1, nc)
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va)
+        m.set_variant(variant)
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+        assert_close(m.spmv_host(x), o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"csr variant {variant} {nr}x{nc}")
+
+
 def test_coo_unsorted_duplicates_and_shift(gpu, orc):
     rng = np.random.default_rng(4)
     for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
