@@ -107,10 +107,11 @@ struct tbsla_matrix {
   float *tile_tail_val32 = nullptr;
   int *d_err = nullptr;              // set by a kernel whose bounded wait gave up
 
-  // PageRank helpers built on first use
-  unsigned char *dangling = nullptr;  // columns without stored entries
-  double *pr_scratch = nullptr;       // reduction partials and scalars
-  size_t pr_scratch_bytes = 0;
+  // PageRank workspace built on first use (pagerank.cu)
+  void *pr_work = nullptr;
+  void (*pr_work_free)(void *) = nullptr;
+  unsigned char *dangling = nullptr;
+  double *pr_scratch = nullptr;
 
   // host-path staging
   cudaStream_t stream = nullptr;

@@ -119,7 +119,8 @@ __device__ __forceinline__ Acc row_sum_thread(const int *__restrict__ colidx, co
   return row_groups<2, V, XT, Acc>(colidx, values, x, f_col, a, b, keep);
 }
 
-// short rows: rows [0, n_rows) when `rows` is NULL, else rows[0..n_rows)
+// short rows: rows [0, n_rows) when `rows` is NULL, else rows[0..n_rows);
+// grid-stride, so that per-block reductions of an epilogue are amortised
 template <typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ rows, int n_rows,
                                                        const int *__restrict__ rowptr,
@@ -127,12 +128,12 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
                                                        const V *__restrict__ values,
                                                        const XT *__restrict__ x, int f_col, Epi epi) {
   using Acc = typename Epi::Acc;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!epi.active()) return;
   typename Epi::State es{};
-  if (t < n_rows) {
+  const uint64_t keep = policy_evict_last();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_rows; t += gridDim.x * blockDim.x) {
     const int r = rows ? __ldg(rows + t) : t;
     const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
-    const uint64_t keep = policy_evict_last();
     epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
   }
   epi.block_done(es, blockIdx.x);
@@ -162,11 +163,12 @@ __global__ void __launch_bounds__(256) csr_warp_kernel(const int4 *__restrict__ 
                                                       const XT *__restrict__ x, int f_col,
                                                       typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (!epi.active()) return;
   typename Epi::State es{};
-  if (w < n_items) {
+  const uint64_t keep = policy_evict_last();
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
     const int4 it = items[w];
-    const uint64_t keep = policy_evict_last();
     const Acc s = range_sum_warp<V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
     if ((threadIdx.x & 31) == 0) {
       if (it.w < 0) epi.emit(it.x, s, es);
@@ -182,6 +184,7 @@ template <typename Epi>
 __global__ void csr_chunk_fixup_kernel(const int2 *__restrict__ huge, int n_huge,
                                        const typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   typename Epi::State es{};
   if (h < n_huge) {

@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(kRowsNT, 3) csr_rows_kernel(const RowBlock *__
   int *s_wsum = s_seg + kRowsMax + 1;
   Acc *s_part = s_val;                // segment sums, after the staged data is consumed
 
+  if (!epi.active()) return;
   const RowBlock d = blocks[blockIdx.x];
   const int r0 = d.x, r1 = d.y, j0 = d.z, huge = d.w;
   const int nrows = r1 - r0;
@@ -210,6 +211,7 @@ template <typename Epi>
 __global__ void csr_huge_fixup_kernel(const int2 *__restrict__ huge_rows, int n_huge,
                                       const typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
   const int h = blockIdx.x * blockDim.x + threadIdx.x;
   typename Epi::State es{};
   if (h < n_huge) {

@@ -8,9 +8,7 @@
 #include <vector>
 
 #include "common.cuh"
-#include "csr_direct.cuh"
-#include "csr_rows.cuh"
-#include "spmv_kernels.cuh"
+#include "product.cuh"
 
 namespace tbsla {
 
@@ -173,6 +171,7 @@ static tbsla_matrix *new_handle(int format) {
 static void free_handle(tbsla_matrix *A) {
   if (!A) return;
   cudaSetDevice(A->device);
+  if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
   for (void *p : A->values) if (p) cudaFree(p);
   void *ptrs[] = {A->idx0, A->idx1, A->row_blocks, A->huge_rows, A->huge_partials, A->huge_partials32,
                   A->short_rows, A->warp_items, A->chunk_rows, A->chunk_partials, A->chunk_partials32,
@@ -187,96 +186,6 @@ static void free_handle(tbsla_matrix *A) {
 }
 
 tbsla_status_t axpy_inplace(double *y, const double *x, int64_t n, cudaStream_t s);
-
-template <typename Acc> Carry<Acc> carry_of(const tbsla_matrix *A);
-template <> Carry<double> carry_of<double>(const tbsla_matrix *A) {
-  return Carry<double>{A->tile_head_row, A->tile_head_val, A->tile_tail_val, A->tile_emitted};
-}
-template <> Carry<float> carry_of<float>(const tbsla_matrix *A) {
-  return Carry<float>{A->tile_head_row, A->tile_head_val32, A->tile_tail_val32, A->tile_emitted};
-}
-
-// ------------------------------------------------------------ launches
-// Dynamic shared memory of csr_rows_kernel (set once per instantiation).
-template <typename V, typename XT, typename Epi> size_t csr_rows_setup() {
-  constexpr size_t smem = csr_rows_smem<typename Epi::Acc>();
-  static bool done = false;
-  if (!done) {
-    cudaFuncSetAttribute(csr_rows_kernel<V, XT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    done = true;
-  }
-  return smem;
-}
-
-template <typename Acc> Acc *huge_partials_of(const tbsla_matrix *A);
-template <> double *huge_partials_of<double>(const tbsla_matrix *A) { return A->huge_partials; }
-template <> float *huge_partials_of<float>(const tbsla_matrix *A) { return A->huge_partials32; }
-template <typename Acc> Acc *chunk_partials_of(const tbsla_matrix *A);
-template <> double *chunk_partials_of<double>(const tbsla_matrix *A) { return A->chunk_partials; }
-template <> float *chunk_partials_of<float>(const tbsla_matrix *A) { return A->chunk_partials32; }
-
-template <typename V, typename XT, typename Epi>
-tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x, Epi epi,
-                              cudaStream_t s) {
-  using Acc = typename Epi::Acc;
-  switch (A->format) {
-  case TBSLA_FMT_CSR:
-    if (A->rows > 0 && A->csr_variant == 0) {
-      KernelTimer kt(A, s);
-      if (A->n_short > 0)
-        csr_short_kernel<V, XT, Epi><<<(A->n_short + 255) / 256, 256, 0, s>>>(A->short_rows, A->n_short, A->idx0,
-                                                                             A->idx1, vals, x, A->f_col, epi);
-      if (A->n_warp_items > 0)
-        csr_warp_kernel<V, XT, Epi><<<(A->n_warp_items + 7) / 8, 256, 0, s>>>(
-            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, chunk_partials_of<Acc>(A), epi);
-      kt.stop();
-      if (A->n_chunk_rows > 0)
-        csr_chunk_fixup_kernel<Epi><<<(A->n_chunk_rows + 127) / 128, 128, 0, s>>>(
-            A->chunk_rows, A->n_chunk_rows, chunk_partials_of<Acc>(A), epi);
-    } else if (A->rows > 0) {
-      const size_t smem = csr_rows_setup<V, XT, Epi>();
-      KernelTimer kt(A, s);
-      csr_rows_kernel<V, XT, Epi><<<A->num_blocks, kRowsNT, smem, s>>>(
-          A->row_blocks, A->idx0, A->idx1, vals, x, A->f_col, huge_partials_of<Acc>(A), epi);
-      kt.stop();
-      if (A->num_huge > 0)
-        csr_huge_fixup_kernel<Epi><<<(A->num_huge + 127) / 128, 128, 0, s>>>(A->huge_rows, A->num_huge,
-                                                                            huge_partials_of<Acc>(A), epi);
-    }
-    break;
-  case TBSLA_FMT_COO:
-  case TBSLA_FMT_SCOO:
-    if (A->stored > 0) {
-      KernelTimer kt(A, s);
-      coo_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
-          A->idx0, A->idx1, vals, x, A->f_col, A->stored, carry_of<Acc>(A), epi);
-      kt.stop();
-      merge_fixup_kernel<Epi><<<(A->num_tiles + 255) / 256, 256, 0, s>>>(A->num_tiles, carry_of<Acc>(A), epi);
-    }
-    break;
-  case TBSLA_FMT_ELL:
-    if (A->rows > 0 && A->max_col > 0) {
-      const int threads = (A->rows + 3) / 4;
-      KernelTimer kt(A, s);
-      ell_kernel<V, XT, Epi><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                 A->rows_pad, A->max_col, epi);
-      kt.stop();
-    }
-    break;
-  case TBSLA_FMT_DENSE:
-    if (A->rows > 0 && A->cols > 0) {
-      const int warps = (A->rows + 3) / 4;
-      KernelTimer kt(A, s);
-      dense_kernel<V, XT, Epi><<<(warps + 7) / 8, 256, 0, s>>>(vals, x, A->rows, A->cols, epi);
-      kt.stop();
-    }
-    break;
-  default:
-    return fail(TBSLA_ERR_INVALID_ARG, "unknown format %d", A->format);
-  }
-  TB_CUDA(cudaGetLastError());
-  return TBSLA_OK;
-}
 
 // y rows the format never writes are zeroed first: COO/SCOO rows without
 // entries, CSR/ELL/DENSE rows past A->rows, and everything when the

@@ -1,0 +1,677 @@
+// pagerank.cu -- PageRank on GB300: fused sweeps, deterministic reductions,
+// CUDA-graph captured iteration, FP64 and mixed precision.
+//
+// A sweep is one SpMV whose epilogue writes the new iterate and accumulates
+// per-thread partial sums (residual, dangling mass, total mass, or the
+// maximum), reduced per block into a partials array; pr_finalize_kernel
+// (one block) reduces the partials in a fixed order and updates the control
+// block (iteration count, stopping flag, the teleport term of the next
+// sweep).  No atomics on values: every result is independent of scheduling.
+// Sweeps run from a CUDA graph of check_every sweeps with ping-pong iterate
+// buffers; kernels of sweeps after convergence return immediately (they test
+// the control block's flag), and the host reads the flag once per graph.
+//
+// Modes
+//   TBSLA_PR_REFERENCE  Matrix::page_rank (src/cpp/matrix/Matrix.cpp:13-61):
+//     b = beta*A b_prev + (1-beta)/n * sum(b_prev); b /= max(b);
+//     err = sum |b - b_prev|; finally b /= sum(b).  With a node list this is
+//     Matrix::personalized_page_rank (Matrix.cpp:63-114).
+//   TBSLA_PR_DANGLING   x = beta*A x + (beta*dangling(x) + (1-beta)*sum(x))/n,
+//     stop when ||x - x_prev||_1 < tol.
+//   mixed precision (DANGLING, precision F32/BF16): FP64 defect correction.
+//     r = G(x) - x by an FP64 sweep (its L1 norm is the stopping quantity),
+//     then e_{j+1} = G~ e_j + r by sweeps on the reduced-precision value store
+//     with FP32 vectors until ||e_{j+1} - e_j||_1 < inner_tol, x += e (FP64).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "product.cuh"
+
+namespace tbsla {
+
+tbsla_status_t spmv_dispatch(const tbsla_matrix *A, tbsla_dtype_t store, tbsla_dtype_t xt, const void *x,
+                             tbsla_dtype_t yt, void *y, int vect_incr, cudaStream_t s);
+
+// ------------------------------------------------------------ control
+struct PrCtl {
+  double beta, tol, inv_n, tele_scale;  // tele_scale: (1-beta)/n or (1-beta)/|P|
+  double add;       // term of the next FP64 sweep (reference: tele; dangling: (b d + (1-b) s)/n)
+  double add_in;    // term of the next inner sweep
+  double maxv;      // reference mode: max of the unnormalised iterate
+  double resid, d, s;
+  double inner_resid, inner_tol;
+  int iter, done, converged, max_iter;
+  int inner_iter, inner_done, inner_max, pad;
+};
+
+enum { kSweepRef = 0, kSweepDang = 1, kSweepInner = 2 };
+
+// Block reduction of three per-thread values into partials[blk*3 + k]
+// (sums, or a maximum for k = 0 when take_max): values go to shared memory,
+// one warp adds them in a fixed order.
+__device__ __forceinline__ void block_reduce3(double a, double b, double c, bool take_max, double *partials,
+                                              int blk) {
+  __shared__ double sh[3][256];
+  const int t = threadIdx.x, nt = blockDim.x;
+  sh[0][t] = a; sh[1][t] = b; sh[2][t] = c;
+  __syncthreads();
+  if (t < 32) {
+    double v[3];
+    for (int k = 0; k < 3; ++k) {
+      double acc = sh[k][t];
+      for (int u = t + 32; u < nt; u += 32) acc = (k == 0 && take_max) ? fmax(acc, sh[k][u]) : acc + sh[k][u];
+      #pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(0xffffffffu, acc, o);
+        acc = (k == 0 && take_max) ? fmax(acc, w) : acc + w;
+      }
+      v[k] = acc;
+    }
+    if (t == 0) {
+      partials[blk * 3 + 0] = v[0];
+      partials[blk * 3 + 1] = v[1];
+      partials[blk * 3 + 2] = v[2];
+    }
+  }
+}
+
+// The sweep epilogue: y[row] = beta*v + add (+ r[row]) and the partial sums.
+template <typename YT, typename AccT> struct PrEpi {
+  using Acc = AccT;
+  struct State {
+    double a = 0, b = 0, c = 0;
+  };
+  YT *y;
+  const YT *xold;               // previous iterate (residual)
+  const YT *rvec;               // inner sweeps: + r
+  const unsigned char *dmask;   // dangling columns (sums b)
+  const unsigned char *tmask;   // reference mode with nodes: teleport only there
+  const double *add;            // device scalar
+  const double *betap;          // device scalar (the damping of this run)
+  const int *done;              // device flag: sweep inactive when set
+  double *partials;
+  int n, mode, part_base;
+  __device__ __forceinline__ bool active() const { return *(volatile const int *)done == 0; }
+  __host__ __device__ void set_part_base(int k) { part_base = k; }
+  __device__ __forceinline__ void emit(int row, Acc v, State &st) const {
+    if (row < 0 || row >= n) return;
+    double val;
+    const double beta = *betap;
+    if (mode == kSweepInner) {
+      const float f = __fmaf_rn((float)beta, (float)v, (float)*add) + (float)rvec[row];
+      val = f;
+      st.a += fabs(val - (double)xold[row]);
+    } else {
+      const double t = (mode == kSweepRef && tmask) ? (tmask[row] ? *add : 0.0) : *add;
+      val = __fma_rn(beta, (double)v, t);
+      if (mode == kSweepRef) st.a = fmax(st.a, val);
+      else st.a += fabs(val - (double)xold[row]);
+    }
+    if (mode != kSweepRef) {
+      if (dmask && dmask[row]) st.b += val;
+      st.c += val;
+    }
+    __stcs(y + row, (YT)val);
+  }
+  __device__ __forceinline__ void block_done(State &st, int blk) const {
+    block_reduce3(st.a, st.b, st.c, mode == kSweepRef, partials, part_base + blk);
+  }
+  __device__ __forceinline__ void fixup_done(State &st, int blk) const { block_done(st, blk); }
+};
+
+// y = beta*(A x) + add (+r) over rows [0, n) from a plain product in `prod`:
+// the path for formats whose kernels do not visit every row
+template <typename YT>
+__global__ void __launch_bounds__(256) pr_affine_kernel(const YT *__restrict__ prod, PrEpi<YT, typename AccOf<YT>::type> epi) {
+  if (!epi.active()) return;
+  typename PrEpi<YT, typename AccOf<YT>::type>::State st;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < epi.n; i += gridDim.x * blockDim.x)
+    epi.emit(i, (typename AccOf<YT>::type)prod[i], st);
+  epi.block_done(st, blockIdx.x);
+}
+
+// reference mode: b /= max; partial sums of |b - b_prev| and of b
+__global__ void __launch_bounds__(256) pr_normalize_kernel(double *__restrict__ b, const double *__restrict__ bprev,
+                                                           int n, const PrCtl *ctl, double *partials) {
+  if (*(volatile const int *)&ctl->done) return;
+  const double m = ctl->maxv;
+  double err = 0, s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = b[i] / m;
+    b[i] = v;
+    err += fabs(v - bprev[i]);
+    s += v;
+  }
+  block_reduce3(err, 0.0, s, false, partials, blockIdx.x);
+}
+
+// reduces partials [0, nparts) and advances the control block
+__global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restrict__ partials, int nparts,
+                                                          PrCtl *ctl, int stage) {
+  const bool inner = stage == 3;
+  if (stage <= 3 && (inner ? *(volatile int *)&ctl->inner_done : *(volatile int *)&ctl->done)) return;
+  __shared__ double sh[3][256];
+  const int t = threadIdx.x;
+  const bool take_max = stage == 0;
+  double a = take_max ? -INFINITY : 0.0, b = 0, c = 0;
+  for (int k = t; k < nparts; k += blockDim.x) {
+    a = take_max ? fmax(a, partials[3 * k]) : a + partials[3 * k];
+    b += partials[3 * k + 1];
+    c += partials[3 * k + 2];
+  }
+  sh[0][t] = a; sh[1][t] = b; sh[2][t] = c;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (t < w) {
+      sh[0][t] = take_max ? fmax(sh[0][t], sh[0][t + w]) : sh[0][t] + sh[0][t + w];
+      sh[1][t] += sh[1][t + w];
+      sh[2][t] += sh[2][t + w];
+    }
+    __syncthreads();
+  }
+  if (t != 0) return;
+  a = sh[0][0]; b = sh[1][0]; c = sh[2][0];
+  if (stage == 7) { ctl->s = c; return; }
+  switch (stage) {
+  case 0:  // reference sweep: maximum of the unnormalised iterate
+    ctl->maxv = a;
+    break;
+  case 1:  // reference normalisation: err = a, sum = c
+    ctl->resid = a;
+    ctl->s = c;
+    ctl->iter += 1;
+    ctl->add = ctl->tele_scale * c;
+    ctl->converged = a < ctl->tol;
+    ctl->done = ctl->converged || ctl->iter >= ctl->max_iter;
+    break;
+  case 2:  // dangling sweep: resid = a, dangling mass = b, sum = c
+    ctl->resid = a;
+    ctl->d = b;
+    ctl->s = c;
+    ctl->iter += 1;
+    ctl->add = (ctl->beta * b + (1.0 - ctl->beta) * c) * ctl->inv_n;
+    ctl->converged = a < ctl->tol;
+    ctl->done = ctl->converged || ctl->iter >= ctl->max_iter;
+    break;
+  case 3:  // inner sweep
+    ctl->inner_resid = a;
+    ctl->inner_iter += 1;
+    ctl->add_in = (ctl->beta * b + (1.0 - ctl->beta) * c) * ctl->inv_n;
+    ctl->inner_done = a < ctl->inner_tol || ctl->inner_iter >= ctl->inner_max;
+    break;
+  case 4:  // initial vector: dangling mass b, sum c (FP64 sweeps)
+    ctl->add = (ctl->beta * b + (1.0 - ctl->beta) * c) * ctl->inv_n;
+    ctl->s = c;
+    break;
+  case 5:  // initial inner vector e0 = r
+    ctl->add_in = (ctl->beta * b + (1.0 - ctl->beta) * c) * ctl->inv_n;
+    break;
+  case 6:  // reference start: tele of b0 = sum(b0) * tele_scale
+    ctl->add = ctl->tele_scale * c;
+    break;
+  case 7:  // plain sum of a vector (final normalisation)
+    ctl->s = c;
+    break;
+  }
+}
+
+// partial (0, dangling mass, sum) of a vector
+template <typename T>
+__global__ void __launch_bounds__(256) pr_mass_kernel(const T *__restrict__ v, int n, const unsigned char *dmask,
+                                                      double *partials) {
+  double d = 0, s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = v[i];
+    if (dmask && dmask[i]) d += x;
+    s += x;
+  }
+  block_reduce3(0.0, d, s, false, partials, blockIdx.x);
+}
+
+__global__ void pr_fill_kernel(double *x, int n, double v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = v;
+}
+
+// r = x1 - x0 in FP32, e0 = r
+__global__ void pr_residual_kernel(const double *__restrict__ x1, const double *__restrict__ x0, float *r,
+                                   float *e, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float d = (float)(x1[i] - x0[i]);
+    r[i] = d;
+    e[i] = d;
+  }
+}
+
+// x += e
+__global__ void pr_correct_kernel(double *__restrict__ x, const float *__restrict__ e, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)e[i];
+}
+
+__global__ void pr_scale_kernel(double *x, int n, const double *sum) {
+  const double s = *sum;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = x[i] / s;
+}
+
+// columns with a nonzero stored value are not dangling
+template <typename V>
+__global__ void pr_dangling_kernel(const int *__restrict__ cols, const V *__restrict__ vals, int64_t n,
+                                   int f_col, int n_col, unsigned char *dmask) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int c = cols[k] - f_col;
+    if (vals[k] != V(0) && c >= 0 && c < n_col) dmask[c] = 0;
+  }
+}
+__global__ void pr_dangling_dense_kernel(const double *__restrict__ a, int rows, int cols, unsigned char *dmask) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < cols; j += gridDim.x * blockDim.x) {
+    bool any = false;
+    for (int i = 0; i < rows && !any; ++i) any = a[(size_t)i * cols + j] != 0.0;
+    if (any) dmask[j] = 0;
+  }
+}
+
+// ------------------------------------------------------------ workspace
+constexpr int kAffineBlocks = 152 * 4;
+
+struct PrWork {
+  int n = 0;
+  double *x[2] = {nullptr, nullptr};  // FP64 iterates
+  double *prod = nullptr;             // plain product (generic path)
+  float *e[2] = {nullptr, nullptr};   // inner iterates
+  float *prod32 = nullptr;
+  float *r = nullptr;
+  unsigned char *dmask = nullptr, *tmask = nullptr;
+  double *partials = nullptr;
+  int nparts = 0;
+  PrCtl *ctl = nullptr;
+  PrCtl *ctl_host = nullptr;          // pinned
+  cudaStream_t stream = nullptr;
+  double *result = nullptr;           // buffer holding the last result
+  // captured graphs: key = (kind, sweeps)
+  struct G { int kind, sweeps, precision; cudaGraphExec_t exec; };
+  std::vector<G> graphs;
+  ~PrWork() {
+    for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+    void *ps[] = {x[0], x[1], prod, e[0], e[1], prod32, r, dmask, tmask, partials, ctl};
+    for (void *p : ps) if (p) cudaFree(p);
+    if (ctl_host) cudaFreeHost(ctl_host);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+static tbsla_status_t pr_alloc(void **p, size_t bytes) {
+  const cudaError_t e = cudaMalloc(p, bytes + 64);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(TBSLA_ERR_OOM, "cudaMalloc(%zu) for PageRank failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return TBSLA_OK;
+}
+
+// blocks of one sweep's partials
+static int sweep_parts(const tbsla_matrix *A, bool fused) {
+  if (!fused) return kAffineBlocks;
+  int p = 0;
+  if (A->n_short > 0) p += short_grid(A->n_short);
+  if (A->n_warp_items > 0) p += warp_grid(A->n_warp_items);
+  if (A->n_chunk_rows > 0) p += fixup_grid(A->n_chunk_rows);
+  return std::max(p, 1);
+}
+
+// the fused path: CSR direct kernels visit every row exactly once
+static bool fused_ok(const tbsla_matrix *A) {
+  return A->format == TBSLA_FMT_CSR && A->csr_variant == 0 && A->rows == A->n_row && A->stored > 0;
+}
+
+static tbsla_status_t pr_setup(tbsla_matrix *A, PrWork **out) {
+  PrWork *W = static_cast<PrWork *>(A->pr_work);
+  if (W) { *out = W; return TBSLA_OK; }
+  W = new PrWork();
+  const int n = A->n_col;
+  W->n = n;
+  tbsla_status_t st = TBSLA_OK;
+  auto alloc = [&](void **p, size_t b) { if (st == TBSLA_OK) st = pr_alloc(p, b); };
+  alloc((void **)&W->x[0], (size_t)n * 8);
+  alloc((void **)&W->x[1], (size_t)n * 8);
+  alloc((void **)&W->prod, (size_t)n * 8);
+  alloc((void **)&W->dmask, (size_t)n);
+  alloc((void **)&W->tmask, (size_t)n);
+  W->nparts = std::max(sweep_parts(A, fused_ok(A)), kAffineBlocks);
+  alloc((void **)&W->partials, (size_t)W->nparts * 3 * 8);
+  alloc((void **)&W->ctl, sizeof(PrCtl));
+  if (st == TBSLA_OK && cudaMallocHost((void **)&W->ctl_host, sizeof(PrCtl)) != cudaSuccess)
+    st = fail(TBSLA_ERR_OOM, "pinned control block");
+  if (st == TBSLA_OK && cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking) != cudaSuccess)
+    st = fail(TBSLA_ERR_CUDA, "stream creation failed");
+  if (st == TBSLA_OK) {
+    // dangling columns: those without a nonzero stored value
+    cudaMemsetAsync(W->dmask, 1, (size_t)n, W->stream);
+    const int g = 152 * 8;
+    switch (A->format) {
+    case TBSLA_FMT_CSR:
+    case TBSLA_FMT_COO:
+    case TBSLA_FMT_SCOO: {
+      const int *cols = A->idx1;
+      if (A->values[0]) pr_dangling_kernel<double><<<g, 256, 0, W->stream>>>(cols, (const double *)A->values[0], A->stored, A->f_col, n, W->dmask);
+      else if (A->values[1]) pr_dangling_kernel<float><<<g, 256, 0, W->stream>>>(cols, (const float *)A->values[1], A->stored, A->f_col, n, W->dmask);
+      break;
+    }
+    case TBSLA_FMT_ELL:
+      if (A->values[0])
+        pr_dangling_kernel<double><<<g, 256, 0, W->stream>>>(A->idx0, (const double *)A->values[0],
+                                                             (int64_t)A->rows_pad * A->max_col, A->f_col, n, W->dmask);
+      break;
+    case TBSLA_FMT_DENSE:
+      if (A->values[0]) pr_dangling_dense_kernel<<<g, 256, 0, W->stream>>>((const double *)A->values[0], A->rows, A->cols, W->dmask);
+      break;
+    }
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(W->stream) != cudaSuccess)
+      st = fail(TBSLA_ERR_CUDA, "PageRank setup kernels failed");
+  }
+  if (st != TBSLA_OK) { delete W; return st; }
+  A->pr_work = W;
+  A->pr_work_free = [](void *p) { delete static_cast<PrWork *>(p); };
+  *out = W;
+  return TBSLA_OK;
+}
+
+static tbsla_status_t pr_inner_buffers(PrWork *W) {
+  if (W->e[0]) return TBSLA_OK;
+  const size_t b = (size_t)W->n * 4;
+  TB_TRY(pr_alloc((void **)&W->e[0], b));
+  TB_TRY(pr_alloc((void **)&W->e[1], b));
+  TB_TRY(pr_alloc((void **)&W->prod32, b));
+  TB_TRY(pr_alloc((void **)&W->r, b));
+  return TBSLA_OK;
+}
+
+// one FP64 sweep x_in -> x_out (mode kSweepRef or kSweepDang) + finalize
+static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const double *x_in, double *x_out,
+                                        int mode, bool with_tmask, cudaStream_t s) {
+  PrEpi<double, double> epi{};
+  epi.y = x_out;
+  epi.xold = x_in;
+  epi.rvec = nullptr;
+  epi.dmask = mode == kSweepDang ? W->dmask : nullptr;
+  epi.tmask = with_tmask ? W->tmask : nullptr;
+  epi.add = &W->ctl->add;
+  epi.betap = &W->ctl->beta;
+  epi.done = &W->ctl->done;
+  epi.partials = W->partials;
+  epi.n = W->n;
+  epi.mode = mode;
+  epi.part_base = 0;
+  int nparts;
+  if (fused_ok(A)) {
+    TB_TRY(launch_product<double, double>(A, static_cast<const double *>(A->values[0]), x_in, epi, s));
+    nparts = sweep_parts(A, true);
+  } else {
+    TB_TRY(spmv_dispatch(A, TBSLA_F64, TBSLA_F64, x_in, TBSLA_F64, W->prod, 0, s));
+    pr_affine_kernel<double><<<kAffineBlocks, 256, 0, s>>>(W->prod, epi);
+    nparts = kAffineBlocks;
+  }
+  if (mode == kSweepRef) {
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, 0);
+    pr_normalize_kernel<<<kAffineBlocks, 256, 0, s>>>(x_out, x_in, W->n, W->ctl, W->partials);
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 1);
+  } else {
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, 2);
+  }
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// one low-precision inner sweep e_in -> e_out + finalize
+static tbsla_status_t enqueue_inner_sweep(const tbsla_matrix *A, PrWork *W, tbsla_dtype_t store, const float *e_in,
+                                          float *e_out, cudaStream_t s) {
+  PrEpi<float, float> epi{};
+  epi.y = e_out;
+  epi.xold = e_in;
+  epi.rvec = W->r;
+  epi.dmask = W->dmask;
+  epi.tmask = nullptr;
+  epi.add = &W->ctl->add_in;
+  epi.betap = &W->ctl->beta;
+  epi.done = &W->ctl->inner_done;
+  epi.partials = W->partials;
+  epi.n = W->n;
+  epi.mode = kSweepInner;
+  int nparts;
+  if (fused_ok(A)) {
+    if (store == TBSLA_F32)
+      TB_TRY(launch_product<float, float>(A, static_cast<const float *>(A->values[1]), e_in, epi, s));
+    else
+      TB_TRY(launch_product<__nv_bfloat16, float>(A, static_cast<const __nv_bfloat16 *>(A->values[2]), e_in, epi, s));
+    nparts = sweep_parts(A, true);
+  } else {
+    TB_TRY(spmv_dispatch(A, store, TBSLA_F32, e_in, TBSLA_F32, W->prod32, 0, s));
+    pr_affine_kernel<float><<<kAffineBlocks, 256, 0, s>>>(W->prod32, epi);
+    nparts = kAffineBlocks;
+  }
+  pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, 3);
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// A graph of `sweeps` sweeps (kind 0: FP64 sweeps from x[0], alternating;
+// kind 1: inner sweeps from e[0], alternating); sweeps is even so that the
+// buffers are back in place after each launch.
+static tbsla_status_t get_graph(const tbsla_matrix *A, PrWork *W, int kind, int sweeps, int precision, int mode,
+                                bool with_tmask, cudaGraphExec_t *exec) {
+  for (auto &g : W->graphs)
+    if (g.kind == kind * 16 + mode * 2 + (with_tmask ? 1 : 0) && g.sweeps == sweeps && g.precision == precision) {
+      *exec = g.exec;
+      return TBSLA_OK;
+    }
+  cudaStream_t s = W->stream;
+  TB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  tbsla_status_t st = TBSLA_OK;
+  for (int k = 0; k < sweeps && st == TBSLA_OK; ++k) {
+    if (kind == 0) st = enqueue_f64_sweep(A, W, W->x[k & 1], W->x[(k + 1) & 1], mode, with_tmask, s);
+    else st = enqueue_inner_sweep(A, W, (tbsla_dtype_t)precision, W->e[k & 1], W->e[(k + 1) & 1], s);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (st != TBSLA_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&ex, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate", __FILE__, __LINE__);
+  W->graphs.push_back({kind * 16 + mode * 2 + (with_tmask ? 1 : 0), sweeps, precision, ex});
+  *exec = ex;
+  return TBSLA_OK;
+}
+
+static tbsla_status_t read_ctl(PrWork *W) {
+  TB_CUDA(cudaMemcpyAsync(W->ctl_host, W->ctl, sizeof(PrCtl), cudaMemcpyDeviceToHost, W->stream));
+  TB_CUDA(cudaStreamSynchronize(W->stream));
+  return TBSLA_OK;
+}
+
+static tbsla_status_t write_ctl(PrWork *W) {
+  TB_CUDA(cudaMemcpyAsync(W->ctl, W->ctl_host, sizeof(PrCtl), cudaMemcpyHostToDevice, W->stream));
+  return TBSLA_OK;
+}
+
+// the FP64 power iteration (reference or dangling mode); result in x[iter % 2]
+static tbsla_status_t run_f64(tbsla_matrix *A, PrWork *W, int mode, bool with_tmask, int check_every) {
+  cudaGraphExec_t ex;
+  TB_TRY(get_graph(A, W, 0, check_every, TBSLA_F64, mode, with_tmask, &ex));
+  while (true) {
+    TB_CUDA(cudaGraphLaunch(ex, W->stream));
+    TB_TRY(read_ctl(W));
+    if (W->ctl_host->done) break;
+  }
+  return TBSLA_OK;
+}
+
+static double *pr_result(PrWork *W) { return W->result; }
+
+}  // namespace tbsla
+
+using namespace tbsla;
+
+static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const int *nodes,
+                                    int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user) {
+  TB_CHECK(A && p, "NULL argument");
+  TB_CHECK(A->n_row == A->n_col, "PageRank needs a square matrix (%d x %d)", A->n_row, A->n_col);
+  TB_CHECK(A->n_col > 0, "empty matrix");
+  TB_CHECK(p->max_iter >= 0, "max_iter < 0");
+  TB_CHECK(p->mode == TBSLA_PR_REFERENCE || p->mode == TBSLA_PR_DANGLING, "unknown PageRank mode %d", p->mode);
+  TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32 || p->precision == TBSLA_BF16, "bad precision");
+  TB_CHECK(p->precision == TBSLA_F64 || p->mode == TBSLA_PR_DANGLING, "reduced precision needs TBSLA_PR_DANGLING");
+  TB_CHECK(A->values[0], "PageRank needs the F64 value store");
+  TB_CHECK(p->precision == TBSLA_F64 || A->values[store_index((tbsla_dtype_t)p->precision)],
+           "the requested reduced-precision value store is not present");
+  TB_CHECK(nodes == nullptr || p->mode == TBSLA_PR_REFERENCE, "node lists are for the reference mode");
+  TB_CUDA(cudaSetDevice(A->device));
+  PrWork *W = nullptr;
+  TB_TRY(pr_setup(A, &W));
+  // kernel timing records events; none inside captured graphs
+  struct TimingOff {
+    tbsla_matrix *A;
+    bool was;
+    ~TimingOff() { A->timing = was; }
+  } timing_off{A, A->timing};
+  A->timing = false;
+  // order after work the caller queued on its stream
+  if (user) {
+    cudaEvent_t ev;
+    TB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, user);
+    cudaStreamWaitEvent(W->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  const int n = W->n;
+  const int K = p->check_every > 0 ? (p->check_every + 1) / 2 * 2 : 8;
+  PrCtl &c = *W->ctl_host;
+  std::memset(&c, 0, sizeof c);
+  c.beta = p->beta;
+  c.tol = p->tol;
+  c.inv_n = 1.0 / n;
+  c.max_iter = p->max_iter;
+  const bool with_tmask = nodes != nullptr;
+  if (with_tmask) {
+    TB_CHECK(n_nodes > 0, "empty node list");
+    std::vector<unsigned char> m((size_t)n, 0);
+    for (int k = 0; k < n_nodes; ++k)
+      if (nodes[k] >= 0 && nodes[k] < n) m[(size_t)nodes[k]] = 1;
+    TB_CUDA(cudaMemcpyAsync(W->tmask, m.data(), (size_t)n, cudaMemcpyHostToDevice, W->stream));
+    TB_CUDA(cudaStreamSynchronize(W->stream));
+    c.tele_scale = (1.0 - p->beta) / n_nodes;
+  } else {
+    c.tele_scale = (1.0 - p->beta) / n;
+  }
+  c.done = p->max_iter == 0;
+  TB_TRY(write_ctl(W));
+  const int g = kAffineBlocks;
+  if (p->mode == TBSLA_PR_REFERENCE) {
+    pr_fill_kernel<<<g, 256, 0, W->stream>>>(W->x[0], n, with_tmask ? 0.25 : 1.0);
+    pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(W->x[0], n, nullptr, W->partials);
+    pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 6);
+  } else {
+    pr_fill_kernel<<<g, 256, 0, W->stream>>>(W->x[0], n, 1.0 / n);
+    pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(W->x[0], n, W->dmask, W->partials);
+    pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 4);
+  }
+  TB_CUDA(cudaGetLastError());
+
+  int f64_sweeps = 0, inner_total = 0;
+  if (p->precision == TBSLA_F64) {
+    if (!c.done) TB_TRY(run_f64(A, W, p->mode == TBSLA_PR_REFERENCE ? kSweepRef : kSweepDang, with_tmask, K));
+    else TB_TRY(read_ctl(W));
+    f64_sweeps = c.iter;
+  } else {
+    TB_TRY(pr_inner_buffers(W));
+    cudaGraphExec_t inner_ex;
+    TB_TRY(get_graph(A, W, 1, K, p->precision, kSweepInner, false, &inner_ex));
+    // defect correction: FP64 sweep for r = G(x) - x, inner solve, x += e
+    const double eta = p->precision == TBSLA_BF16 ? 0.05 : 0.01;
+    while (true) {
+      TB_TRY(enqueue_f64_sweep(A, W, W->x[0], W->x[1], kSweepDang, false, W->stream));
+      TB_TRY(read_ctl(W));
+      ++f64_sweeps;
+      if (c.done) break;
+      // r = x1 - x0, e0 = r; inner solve to ||e_{j+1}-e_j|| < eta ||r||
+      pr_residual_kernel<<<g, 256, 0, W->stream>>>(W->x[1], W->x[0], W->r, W->e[0], n);
+      pr_mass_kernel<float><<<g, 256, 0, W->stream>>>(W->e[0], n, W->dmask, W->partials);
+      c.inner_iter = 0;
+      c.inner_done = 0;
+      c.inner_tol = eta * c.resid;
+      c.inner_max = 4 * K * 16;
+      // only the inner fields change: copy the control block back
+      TB_TRY(write_ctl(W));
+      pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 5);
+      while (true) {
+        TB_CUDA(cudaGraphLaunch(inner_ex, W->stream));
+        TB_TRY(read_ctl(W));
+        if (c.inner_done) break;
+      }
+      inner_total += c.inner_iter;
+      pr_correct_kernel<<<g, 256, 0, W->stream>>>(W->x[0], W->e[c.inner_iter & 1], n);
+      // the next FP64 sweep needs the teleport term of the corrected x
+      pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(W->x[0], n, W->dmask, W->partials);
+      pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 4);
+      TB_CUDA(cudaGetLastError());
+    }
+  }
+  // result buffer: FP64 runs end in x[iter % 2]; the mixed run in x[1], the
+  // output G(x) of its last FP64 sweep
+  W->result = p->precision == TBSLA_F64 ? W->x[c.iter & 1] : W->x[1];
+  double *xr = W->result;
+  if (p->mode == TBSLA_PR_REFERENCE || p->precision != TBSLA_F64) {
+    // reference: b /= sum(b) (Matrix.cpp:52-59); mixed: sum-normalise
+    const double keep_s = c.s;
+    pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(xr, n, nullptr, W->partials);
+    pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 7);
+    pr_scale_kernel<<<g, 256, 0, W->stream>>>(xr, n, &W->ctl->s);
+    (void)keep_s;
+  }
+  if (d_out) TB_CUDA(cudaMemcpyAsync(d_out, xr, (size_t)n * 8, cudaMemcpyDeviceToDevice, W->stream));
+  TB_CUDA(cudaGetLastError());
+  TB_CUDA(cudaStreamSynchronize(W->stream));
+  if (res) {
+    TB_TRY(read_ctl(W));
+    res->iterations = p->precision == TBSLA_F64 ? c.iter : f64_sweeps + inner_total;
+    res->iterations_f64 = f64_sweeps;
+    res->residual = c.resid;
+    res->converged = c.converged;
+  }
+  return TBSLA_OK;
+}
+
+extern "C" {
+
+tbsla_status_t tbsla_pagerank(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, double *d_out,
+                              tbsla_pagerank_result_t *result, void *stream) {
+  return pagerank_impl(const_cast<tbsla_matrix *>(A), p, nullptr, 0, d_out, result, (cudaStream_t)stream);
+}
+
+tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, double *out,
+                                   int64_t n_out, tbsla_pagerank_result_t *result) {
+  TB_CHECK(A && out, "NULL argument");
+  TB_CHECK(n_out >= A->n_col, "output has %lld entries, need %d", (long long)n_out, A->n_col);
+  std::lock_guard<std::mutex> lk(A->host_mu);
+  TB_TRY(pagerank_impl(A, p, nullptr, 0, nullptr, result, nullptr));
+  PrWork *W = static_cast<PrWork *>(A->pr_work);
+  TB_CUDA(cudaMemcpy(out, pr_result(W), (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                                const int *nodes, int n_nodes, double *out, int64_t n_out,
+                                                tbsla_pagerank_result_t *result) {
+  TB_CHECK(A && out && nodes, "NULL argument");
+  TB_CHECK(n_out >= A->n_col, "output has %lld entries, need %d", (long long)n_out, A->n_col);
+  std::lock_guard<std::mutex> lk(A->host_mu);
+  tbsla_pagerank_params_t q = *p;
+  q.mode = TBSLA_PR_REFERENCE;
+  q.precision = TBSLA_F64;
+  TB_TRY(pagerank_impl(A, &q, nodes, n_nodes, nullptr, result, nullptr));
+  PrWork *W = static_cast<PrWork *>(A->pr_work);
+  TB_CUDA(cudaMemcpy(out, pr_result(W), (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
+  return TBSLA_OK;
+}
+
+}  // extern "C"

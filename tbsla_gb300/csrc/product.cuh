@@ -1,0 +1,127 @@
+// product.cuh -- launches of the SpMV kernels of every format with an
+// epilogue functor (shared by the plain products and PageRank).
+//
+// Every epilogue provides:
+//   active()             false once its computation is finished (PageRank
+//                        sweeps after convergence): kernels return at once;
+//   emit(row, v, state)  receives each finished row exactly once;
+//   block_done / fixup_done(state, block)  per-block reduction hooks;
+//   set_part_base(k)     offset of the launch's blocks in a partials array.
+#pragma once
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "csr_direct.cuh"
+#include "csr_rows.cuh"
+#include "spmv_kernels.cuh"
+
+namespace tbsla {
+
+// grid of the grid-stride CSR kernels: one pass over the rows, at most
+// kStrideBlocks blocks (each thread then takes several rows)
+constexpr int kStrideBlocks = 152 * 16;
+inline int short_grid(int n_short) { return std::max(1, std::min((n_short + 255) / 256, kStrideBlocks)); }
+inline int warp_grid(int n_items) { return std::max(1, std::min((n_items + 7) / 8, kStrideBlocks)); }
+inline int fixup_grid(int n) { return std::max(1, (n + 127) / 128); }
+
+template <typename Acc> inline Carry<Acc> carry_of(const tbsla_matrix *A);
+template <> inline Carry<double> carry_of<double>(const tbsla_matrix *A) {
+  return Carry<double>{A->tile_head_row, A->tile_head_val, A->tile_tail_val, A->tile_emitted};
+}
+template <> inline Carry<float> carry_of<float>(const tbsla_matrix *A) {
+  return Carry<float>{A->tile_head_row, A->tile_head_val32, A->tile_tail_val32, A->tile_emitted};
+}
+
+// ------------------------------------------------------------ launches
+// Dynamic shared memory of csr_rows_kernel (set once per instantiation).
+template <typename V, typename XT, typename Epi> size_t csr_rows_setup() {
+  constexpr size_t smem = csr_rows_smem<typename Epi::Acc>();
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(csr_rows_kernel<V, XT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    done = true;
+  }
+  return smem;
+}
+
+template <typename Acc> inline Acc *huge_partials_of(const tbsla_matrix *A);
+template <> inline double *huge_partials_of<double>(const tbsla_matrix *A) { return A->huge_partials; }
+template <> inline float *huge_partials_of<float>(const tbsla_matrix *A) { return A->huge_partials32; }
+template <typename Acc> inline Acc *chunk_partials_of(const tbsla_matrix *A);
+template <> inline double *chunk_partials_of<double>(const tbsla_matrix *A) { return A->chunk_partials; }
+template <> inline float *chunk_partials_of<float>(const tbsla_matrix *A) { return A->chunk_partials32; }
+
+template <typename V, typename XT, typename Epi>
+tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x, Epi epi,
+                              cudaStream_t s) {
+  using Acc = typename Epi::Acc;
+  switch (A->format) {
+  case TBSLA_FMT_CSR:
+    if (A->rows > 0 && A->csr_variant == 0) {
+      KernelTimer kt(A, s);
+      int base = 0;
+      if (A->n_short > 0) {
+        epi.set_part_base(base);
+        base += short_grid(A->n_short);
+        csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short), 256, 0, s>>>(A->short_rows, A->n_short, A->idx0,
+                                                                           A->idx1, vals, x, A->f_col, epi);
+      }
+      if (A->n_warp_items > 0) {
+        epi.set_part_base(base);
+        base += warp_grid(A->n_warp_items);
+        csr_warp_kernel<V, XT, Epi><<<warp_grid(A->n_warp_items), 256, 0, s>>>(
+            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, chunk_partials_of<Acc>(A), epi);
+      }
+      kt.stop();
+      if (A->n_chunk_rows > 0) {
+        epi.set_part_base(base);
+        csr_chunk_fixup_kernel<Epi><<<fixup_grid(A->n_chunk_rows), 128, 0, s>>>(
+            A->chunk_rows, A->n_chunk_rows, chunk_partials_of<Acc>(A), epi);
+      }
+    } else if (A->rows > 0) {
+      const size_t smem = csr_rows_setup<V, XT, Epi>();
+      KernelTimer kt(A, s);
+      csr_rows_kernel<V, XT, Epi><<<A->num_blocks, kRowsNT, smem, s>>>(
+          A->row_blocks, A->idx0, A->idx1, vals, x, A->f_col, huge_partials_of<Acc>(A), epi);
+      kt.stop();
+      if (A->num_huge > 0)
+        csr_huge_fixup_kernel<Epi><<<(A->num_huge + 127) / 128, 128, 0, s>>>(A->huge_rows, A->num_huge,
+                                                                            huge_partials_of<Acc>(A), epi);
+    }
+    break;
+  case TBSLA_FMT_COO:
+  case TBSLA_FMT_SCOO:
+    if (A->stored > 0) {
+      KernelTimer kt(A, s);
+      coo_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
+          A->idx0, A->idx1, vals, x, A->f_col, A->stored, carry_of<Acc>(A), epi);
+      kt.stop();
+      merge_fixup_kernel<Epi><<<(A->num_tiles + 255) / 256, 256, 0, s>>>(A->num_tiles, carry_of<Acc>(A), epi);
+    }
+    break;
+  case TBSLA_FMT_ELL:
+    if (A->rows > 0 && A->max_col > 0) {
+      const int threads = (A->rows + 3) / 4;
+      KernelTimer kt(A, s);
+      ell_kernel<V, XT, Epi><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                 A->rows_pad, A->max_col, epi);
+      kt.stop();
+    }
+    break;
+  case TBSLA_FMT_DENSE:
+    if (A->rows > 0 && A->cols > 0) {
+      const int warps = (A->rows + 3) / 4;
+      KernelTimer kt(A, s);
+      dense_kernel<V, XT, Epi><<<(warps + 7) / 8, 256, 0, s>>>(vals, x, A->rows, A->cols, epi);
+      kt.stop();
+    }
+    break;
+  default:
+    return fail(TBSLA_ERR_INVALID_ARG, "unknown format %d", A->format);
+  }
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+}  // namespace tbsla

@@ -39,6 +39,8 @@ template <typename YT, typename AccT> struct StoreEpi {
     int o = row + shift;
     if (o >= 0 && o < n_out) __stcs(y + o, (YT)v);  // streaming: keep L2 for x
   }
+  __device__ __forceinline__ bool active() const { return true; }
+  __host__ __device__ void set_part_base(int) {}
   __device__ __forceinline__ void block_done(State &, int) const {}
   __device__ __forceinline__ void fixup_done(State &, int) const {}
 };
@@ -55,6 +57,8 @@ template <typename AccT> struct AddXEpi {
     int o = row + shift;
     if (o >= 0 && o < n_out) __stcs(y + o, (double)v + x[o]);
   }
+  __device__ __forceinline__ bool active() const { return true; }
+  __host__ __device__ void set_part_base(int) {}
   __device__ __forceinline__ void block_done(State &, int) const {}
   __device__ __forceinline__ void fixup_done(State &, int) const {}
 };
@@ -160,6 +164,7 @@ __device__ __forceinline__ void stage_tile(const V *__restrict__ vals, const int
 template <typename Epi>
 __global__ void merge_fixup_kernel(int num_tiles, Carry<typename Epi::Acc> carry, Epi epi) {
   using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   typename Epi::State es{};
   if (t < num_tiles) {
@@ -195,6 +200,7 @@ __global__ void __launch_bounds__(NT) coo_merge_kernel(const int *__restrict__ r
   __shared__ unsigned char s_emit[NT];
   __shared__ int s_misc[NT / 32 + 2];
 
+  if (!epi.active()) return;
   const int t = blockIdx.x;
   const int64_t e0 = (int64_t)t * TILE;
   const int n_t = (int)min((int64_t)TILE, nnz - e0);
@@ -267,6 +273,7 @@ __global__ void __launch_bounds__(256) ell_kernel(const int *__restrict__ cols,
                                                   const XT *__restrict__ x, int f_col, int rows,
                                                   int rows_pad, int max_col, Epi epi) {
   using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
   const int r0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
   typename Epi::State es{};
   if (r0 < rows) {
@@ -302,6 +309,7 @@ __global__ void __launch_bounds__(256) dense_kernel(const V *__restrict__ a,
                                                     Epi epi) {
   using Acc = typename Epi::Acc;
   constexpr int RW = 4;
+  if (!epi.active()) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int r0 = warp * RW;

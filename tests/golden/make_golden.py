@@ -123,9 +123,9 @@ def main() -> None:
                     b2, it2 = m.page_rank(1e-10, 0.85, 500)
                     p, itp = m.personalized_page_rank(0.85, 0.01, 10, [1, 3])
                     prs.append({"format": f, "shape": [nr, nc, c], "q": q, "seed": s,
-                                "swapped": {"it": it, "b": [repr(v) for v in b]},
-                                "tight": {"it": it2, "b": [repr(v) for v in b2]},
-                                "ppr": {"it": itp, "b": [repr(v) for v in p]}})
+                                "swapped": {"it": it, "b": [repr(float(v)) for v in b]},
+                                "tight": {"it": it2, "b": [repr(float(v)) for v in b2]},
+                                "ppr": {"it": itp, "b": [repr(float(v)) for v in p]}})
     out["page_rank"] = prs
 
     # cfg1: cqmat n=1e5 c=10 q=0.1 seed 0, CSR
@@ -136,7 +136,7 @@ def main() -> None:
     R.set_threads(8)
     y = m.spmv(x)
     out["cfg1"] = {"arrays": arrays_record(a, big=True), "x_seed": 0, "y_fnv": fnv_fast(y),
-                   "y_sum": repr(float(y.sum())), "y_head": [repr(v) for v in y[:8]]}
+                   "y_sum": repr(float(y.sum())), "y_head": [repr(float(v)) for v in y[:8]]}
     # cfg2: cqmat n=2^24 c=16 q=0.1 seed 0, CSR (fingerprints only)
     m = R.fill_cqmat("CSR", 1 << 24, 1 << 24, 16, 0.1, 0)
     out["cfg2"] = {"arrays": arrays_record(m.arrays, big=True)}

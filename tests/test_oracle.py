@@ -135,11 +135,11 @@ def test_spmv_iota_and_page_rank_match_golden(orc, golden):
         nr, nc, c = rec["shape"]
         m = orc.fill_cqmat_stochastic(rec["format"], nr, nc, c, rec["q"], rec["seed"])
         b, it = m.page_rank(0.85, 0.01, 10)
-        assert it == rec["swapped"]["it"] and [repr(v) for v in b] == rec["swapped"]["b"]
+        assert it == rec["swapped"]["it"] and [repr(float(v)) for v in b] == rec["swapped"]["b"]
         b, it = m.page_rank(1e-10, 0.85, 500)
-        assert it == rec["tight"]["it"] and [repr(v) for v in b] == rec["tight"]["b"]
+        assert it == rec["tight"]["it"] and [repr(float(v)) for v in b] == rec["tight"]["b"]
         b, it = m.personalized_page_rank(0.85, 0.01, 10, [1, 3])
-        assert it == rec["ppr"]["it"] and [repr(v) for v in b] == rec["ppr"]["b"]
+        assert it == rec["ppr"]["it"] and [repr(float(v)) for v in b] == rec["ppr"]["b"]
 
 
 def test_cfg1_matches_golden(orc, golden):

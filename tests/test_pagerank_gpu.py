@@ -1,0 +1,105 @@
+"""PageRank on the GPU against the oracle, through the C ABI.
+
+Reference mode (Matrix::page_rank / personalized_page_rank, Matrix.cpp:13-114):
+same iteration count as the oracle and vectors equal to 1e-12 (the GPU sums
+in another order).  Dangling mode: FP64 and mixed precision against the
+oracle's FP64 iteration run to a tighter tolerance, L1 distance <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from test_oracle import FORMATS
+
+pytestmark = pytest.mark.gpu
+
+
+def rmat_csr_oracle(orc, scale, m, seed):
+    """The R-MAT PageRank matrix built in numpy from the oracle's edges."""
+    src, dst = orc.rmat_edges(scale, m, seed=seed)
+    n = 1 << scale
+    key = np.unique((dst.astype(np.int64) << scale) | src.astype(np.int64))
+    d = (key >> scale).astype(np.int32)
+    s = (key & (n - 1)).astype(np.int32)
+    rowptr = np.zeros(n + 1, np.int32)
+    np.add.at(rowptr, d + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    outdeg = np.bincount(s, minlength=n)
+    values = 1.0 / outdeg[s]
+    dangling = (outdeg == 0).astype(np.uint8)
+    return rowptr, s, values, dangling
+
+
+def test_rmat_matrix_matches_oracle(gpu, orc):
+    for (scale, m, seed) in [(6, 300, 1), (10, 16 << 10, 1), (12, 16 << 12, 7)]:
+        A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=seed)
+        rp, ci, va = A.csr_download()
+        orp, oci, ova, _ = rmat_csr_oracle(orc, scale, m, seed)
+        assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+        assert np.array_equal(va, ova)
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_reference_mode_matches_golden_and_oracle(gpu, orc, golden, fmt):
+    for rec in golden["page_rank"]:
+        if rec["format"] != fmt:
+            continue
+        nr, nc, c = rec["shape"]
+        g = gpu.generate(fmt, "cqmat_stochastic", nr, nc, c, rec["q"], rec["seed"])
+        m = gpu.DeviceMatrix.from_generated(g)
+        for key, (eps, beta, mx) in (("swapped", (0.85, 0.01, 10)), ("tight", (1e-10, 0.85, 500))):
+            b, r = m.pagerank_host(beta=beta, tol=eps, max_iter=mx, mode=gpu.PR_REFERENCE)
+            ref = np.array([float(v) for v in rec[key]["b"]])
+            assert r.iterations == rec[key]["it"], (fmt, rec["shape"], key, r.iterations, rec[key]["it"])
+            np.testing.assert_allclose(b, ref, rtol=1e-12, atol=1e-15)
+        p, r = m.personalized_pagerank_host([1, 3], beta=0.01, tol=0.85, max_iter=10)
+        ref = np.array([float(v) for v in rec["ppr"]["b"]])
+        assert r.iterations == rec["ppr"]["it"]
+        np.testing.assert_allclose(p, ref, rtol=1e-12, atol=1e-15)
+
+
+def test_reference_mode_larger_against_oracle(gpu, orc):
+    for fmt in ("CSR", "ELL", "COO"):
+        g = gpu.generate(fmt, "cqmat_stochastic", 20000, 20000, 12, 0.3, 1)
+        m = gpu.DeviceMatrix.from_generated(g)
+        o = orc.from_layout(fmt, g.geom, g.nnz, g.values, g.idx0, g.idx1)
+        b, r = m.pagerank_host(beta=0.85, tol=1e-6, max_iter=200, mode=gpu.PR_REFERENCE)
+        bo, it = o.page_rank(1e-6, 0.85, 200)
+        assert r.iterations == it
+        assert np.abs(b - bo).sum() < 1e-12
+        p, r = m.personalized_pagerank_host([5, 77, 9000, 5], beta=0.85, tol=1e-6, max_iter=200)
+        po, it = o.personalized_page_rank(1e-6, 0.85, 200, [5, 77, 9000, 5])
+        assert r.iterations == it
+        assert np.abs(p - po).sum() < 1e-12
+
+
+@pytest.mark.parametrize("scale", [10, 14])
+def test_dangling_mode_fp64_and_mixed(gpu, orc, scale):
+    m = 16 << scale
+    A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=1,
+                                       stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
+    rp, ci, va, dang = rmat_csr_oracle(orc, scale, m, 1)
+    xo, it_o, res_o = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 1e-14, 5000)
+    assert res_o < 1e-14
+    # same number of sweeps from the same start: the FP64 iterates agree
+    x8, r8 = A.pagerank_host(beta=0.85, tol=0.0, max_iter=8, mode=gpu.PR_DANGLING)
+    x8o, _, _ = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 0.0, 8)
+    assert r8.iterations == 8 and np.abs(x8 - x8o).sum() < 1e-13
+    for prec in (gpu.F64, gpu.F32, gpu.BF16):
+        x, r = A.pagerank_host(beta=0.85, tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
+        assert r.converged, prec
+        assert abs(x.sum() - 1.0) < 1e-12
+        err = np.abs(x - xo).sum()
+        assert err < 1e-10, (prec, err, r.iterations, r.iterations_f64)
+
+
+def test_pagerank_argument_checks(gpu):
+    g = gpu.generate("CSR", "cqmat_stochastic", 50, 40, 5, 0.1, 0)
+    m = gpu.DeviceMatrix.from_generated(g)
+    with pytest.raises(gpu.TbslaError):
+        m.pagerank_host()  # not square
+    g = gpu.generate("CSR", "cqmat_stochastic", 50, 50, 5, 0.1, 0)
+    m = gpu.DeviceMatrix.from_generated(g)
+    with pytest.raises(gpu.TbslaError):
+        m.pagerank_host(precision=gpu.BF16)  # no BF16 store
+    with pytest.raises(gpu.TbslaError):
+        m.pagerank_host(mode=gpu.PR_REFERENCE, precision=gpu.F32)
