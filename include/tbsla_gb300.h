@@ -152,6 +152,24 @@ tbsla_status_t tbsla_a_axpx(const tbsla_matrix_t *A, const double *d_x, double *
 tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *r,
                                  int64_t nr, int vect_incr);
 
+/* y = A x for row-sorted COO triplets already on the device, without
+ * allocating any memory.  This entry point has no counterpart in the
+ * reference.  It is for callers that cannot call cudaMalloc: their device
+ * memory is owned by another allocator (a framework's caching pool or a
+ * fixed arena), or they cannot afford the device-wide synchronisation that
+ * cudaMalloc / cudaFree may cause.  Inputs and outputs are the caller's
+ * device buffers: d_row (nondecreasing rows in [0, n_row)), d_col (columns in
+ * [0, n_col)), d_values, d_x (n_col), d_y (n_row, cleared by the call).  The
+ * product's only scratch is a fixed array inside the library (344 KiB per
+ * device, held until exit), which limits nnz to 37,748,736 stored entries;
+ * larger nnz returns TBSLA_ERR_INVALID_ARG without launching anything.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and
+ * should come before any stream capture on that device.  All calls share the
+ * array: calls that overlap on the GPU race and must be ordered by the
+ * caller. */
+tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t nnz, const int *d_row, const int *d_col,
+                                      const double *d_values, const double *d_x, double *d_y, void *stream);
+
 /* ----------------------------------------------------------- PageRank */
 typedef enum {
   /* Matrix::page_rank (Matrix.cpp:13-61): b0 = 1; b = beta*A b + (1-beta)/n *

@@ -1,0 +1,91 @@
+// noalloc.cu -- a COO SpMV entry point that allocates no memory.
+//
+// Some callers cannot call cudaMalloc: their device memory is owned by
+// another allocator (a framework's caching pool or a fixed arena that has
+// already reserved it), or they cannot afford the device-wide
+// synchronisation that cudaMalloc and cudaFree may cause in the middle of a
+// pipeline.  tbsla_coo_spmv_noalloc serves them: the caller passes the
+// row-sorted triplets, x and y as device pointers, and the only scratch the
+// product needs -- the per-tile carries of the merge-path COO kernel -- lives
+// in the file-scope device array below, which every GPU that loads this
+// library holds until the process exits.
+//
+// Set-up: the first call on a device, with that device current, looks the
+// array's device address up with cudaGetSymbolAddress (in host code the
+// array's name is only a host-side stand-in, not a device address).  That
+// first call should therefore come before any stream capture on the device.
+//
+// Sharing: every call uses the same array.  Each call overwrites every carry
+// it reads before reading it (nothing has to start at zero; y is cleared by
+// the call), but two calls that overlap on the GPU -- on different streams,
+// or from different host threads -- race on the array and must be ordered by
+// the caller.
+#include <mutex>
+
+#include "product.cuh"
+
+namespace tbsla {
+
+// at most kNoAllocMaxTiles tiles of kMergeTile stored entries
+constexpr int kNoAllocMaxTiles = 16384;
+constexpr int64_t kNoAllocMaxEntries = (int64_t)kNoAllocMaxTiles * kMergeTile;  // 37,748,736
+
+// carries: head_row (int), emitted (byte), head_val and tail_val (double)
+constexpr size_t kOffHeadRow = 0;
+constexpr size_t kOffEmitted = kOffHeadRow + (size_t)kNoAllocMaxTiles * sizeof(int);
+constexpr size_t kOffHeadVal = (kOffEmitted + (size_t)kNoAllocMaxTiles + 255) / 256 * 256;
+constexpr size_t kOffTailVal = kOffHeadVal + (size_t)kNoAllocMaxTiles * sizeof(double);
+constexpr size_t kNoAllocBytes = kOffTailVal + (size_t)kNoAllocMaxTiles * sizeof(double);  // 344,064 B
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// device address of the scratch array on the current device (looked up once)
+static tbsla_status_t noalloc_scratch(unsigned char **out) {
+  int dev = 0;
+  TB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(TBSLA_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return TBSLA_OK;
+}
+
+}  // namespace tbsla
+
+using namespace tbsla;
+
+extern "C" tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t nnz, const int *d_row,
+                                                 const int *d_col, const double *d_values, const double *d_x,
+                                                 double *d_y, void *stream) {
+  TB_CHECK(n_row >= 0 && n_col >= 0 && nnz >= 0, "negative size");
+  TB_CHECK(nnz <= kNoAllocMaxEntries,
+           "nnz %lld exceeds the %lld stored entries the allocation-free COO product can hold "
+           "(%d tiles of %d); use tbsla_coo_create + tbsla_spmv",
+           (long long)nnz, (long long)kNoAllocMaxEntries, kNoAllocMaxTiles, kMergeTile);
+  TB_CHECK(nnz == 0 || (d_row && d_col && d_values && d_x), "NULL input array");
+  TB_CHECK(d_y || n_row == 0, "y is NULL");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char *scratch = nullptr;
+  TB_TRY(noalloc_scratch(&scratch));
+  if (n_row > 0) TB_CUDA(cudaMemsetAsync(d_y, 0, (size_t)n_row * sizeof(double), s));
+  if (nnz == 0) return TBSLA_OK;
+  const int tiles = (int)((nnz + kMergeTile - 1) / kMergeTile);
+  const Carry<double> carry{reinterpret_cast<int *>(scratch + kOffHeadRow),
+                            reinterpret_cast<double *>(scratch + kOffHeadVal),
+                            reinterpret_cast<double *>(scratch + kOffTailVal), scratch + kOffEmitted};
+  StoreEpi<double, double> epi{d_y, n_row, 0};
+  coo_merge_kernel<kMergeThreads, kMergeItems, double, double, StoreEpi<double, double>>
+      <<<tiles, kMergeThreads, 0, s>>>(d_row, d_col, d_values, d_x, 0, nnz, carry, epi);
+  merge_fixup_kernel<StoreEpi<double, double>><<<(tiles + 255) / 256, 256, 0, s>>>(tiles, carry, epi);
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
