@@ -1,19 +1,26 @@
-"""Benchmark of the TBSLA SpMV path on GB300 (one JSON line on stdout).
+"""Benchmark of the TBSLA SpMV / PageRank path on GB300 (one JSON line on stdout).
 
-Headline workload: CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24,
-c = 16, q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of
-algorithmic traffic per product).  A "step" is one product over the resident
-matrix.  ``value`` is achieved GB/s (algorithmic bytes / device time, inputs
-resident in HBM); ``e2e`` is the same metric through the C ABI's host-vector
-call (tbsla_spmv_host: pinned x in, y out, copies inside the timed region).
+Headline (``value``): CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24, c = 16,
+q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of algorithmic traffic per
+product), in GB/s of algorithmic bytes over device time with the matrix and x
+resident in HBM.  A "step" is one product.  ``e2e`` is the same metric through
+the C ABI's host-vector call (tbsla_spmv_host): pinned x copied in, y copied
+out, both inside the timed region.
+
+Also reported (single-GPU runs): the format sweep of the same configuration
+(ELL/COO/SCOO FP64, CSR FP32/BF16 stores, DENSE n = 32768, cdiag n = 2^26) and
+PageRank on the R-MAT graph 2^24 nodes / 2^28 edge draws, (a,b,c,d) = (0.57,
+0.19, 0.19, 0.05), seed 1, damping 0.85, dangling mass redistributed, stopped at
+L1 residual 1e-10: time to tolerance in FP64 and with FP32 / BF16 stored values
+plus FP64 refinement, and each result's L1 distance to an FP64 solve at 1e-13.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-``--impl reference`` times the reference's CPU path (MatrixCSR::Ax with
-OpenMP over rows, src/cpp/matrix/MatrixCSR.cpp:129-140) as restated in
-oracle/ (the reference's sources are not on the GPU host) on all host cores.
-Under torchrun each rank runs an independent replica on its own GPU
-(the path has no data exchange); rank 0 prints the line.
+``--impl reference`` times the reference's CPU product (MatrixCSR::Ax, OpenMP
+over rows, src/cpp/matrix/MatrixCSR.cpp:129-140) as restated in oracle/ on all
+host cores (the reference's own sources are not on the GPU host).  Under
+torchrun every rank runs an independent replica on its own GPU (the path has no
+data exchange); rank 0 prints the line.
 """
 from __future__ import annotations
 
@@ -34,10 +41,10 @@ sys.path.insert(0, ROOT)
 N_HEADLINE = 1 << 24
 C_HEADLINE = 16
 Q_HEADLINE = 0.1
-METRIC = "SpMV GB/s (% HBM peak)"
-# DRAM bytes per launch of csr_merge_kernel on this workload from the ncu
-# capture summarised in profiles/csr_merge_kernel_cqmat_2p24.md (None until
-# captured)
+METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
+WORKLOAD = "cqmat CSR FP64 SpMV n=2^24 c=16 q=0.1 seed=0"
+# DRAM bytes (read + write) of one csr_short_kernel launch on this workload,
+# from the ncu capture summarised in profiles/csr_short_kernel_cqmat_2p24.md
 NCU_TRAFFIC_BYTES = None
 
 
@@ -48,11 +55,9 @@ def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):
 
 
 def peaks():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        with open(path) as fh:
-            p = json.load(fh)
-        return float(p["hbm_gbs"]), "measured"
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
 
@@ -65,10 +70,7 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device_index: int):
-        self.dev = device_index
-        self.rows = []
-        self.proc = None
-        self.thread = None
+        self.dev, self.rows, self.proc, self.thread = device_index, [], None, None
 
     def start(self):
         try:
@@ -98,16 +100,19 @@ class ClockSampler:
             self.thread.join(timeout=2)
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        pw = [num(r[3]) for r in self.rows if num(r[3]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
-            for k, nm in enumerate(names):
-                if r[5 + k].lower().startswith("active"):
-                    reasons.add(nm)
+        reasons = sorted({nm for r in self.rows for k, nm in enumerate(names) if r[5 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "power_w_max": max(pw) if pw else None, "reasons": reasons, "samples": len(self.rows)}
 
 
 def dist_setup():
@@ -140,8 +145,7 @@ def cpu_spmv_baseline(g, steps: int, threads: int):
     """The reference's CSR product restated in oracle/ (OpenMP over rows) on
     the full matrix; returns (GB/s, seconds per product)."""
     from oracle.oracle import Oracle
-    orc = Oracle()
-    m = orc.from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
+    m = Oracle().from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
     x = np.random.default_rng(1).uniform(-1, 1, g.n_col)
     m.spmv(x, threads=threads)  # first touch
     ts = []
@@ -153,30 +157,113 @@ def cpu_spmv_baseline(g, steps: int, threads: int):
     return csr_bytes(g.n_row, g.n_col, g.values.size) / t / 1e9, t
 
 
-def run_reference(args, world, rank, pg):
+def run_reference(args, world, rank):
     if rank != 0:
         return
     from tbsla_gb300 import build, capi
-    build.build()
     from oracle.oracle import build as obuild
+    build.build()
     obuild(ref=False)
     threads = os.cpu_count() or 1
-    t0 = time.time()
     g = capi.generate("CSR", "cqmat", N_HEADLINE, N_HEADLINE, C_HEADLINE, Q_HEADLINE, 0)
-    gen_s = time.time() - t0
-    for _ in range(args.warmup):
-        pass
     gbs, t = cpu_spmv_baseline(g, max(args.steps, 1), threads)
     line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "cqmat CSR FP64 SpMV n=2^24 c=16 q=0.1 seed=0", "n": N_HEADLINE,
-                       "nnz": int(g.values.size), "format": "CSR"},
+            "config": {"workload": WORKLOAD, "n": N_HEADLINE, "nnz": int(g.values.size), "format": "CSR"},
             "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                              "sample": f"full matrix, median of {max(args.steps, 1)} products"},
-            "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "setup_s": round(gen_s, 2)}
+            "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def time_product(capi, A, store, vt, n_row, n_col, reps=10):
+    """Device time of one product (CUDA events on the launching stream)."""
+    import torch
+    tdt = torch.float64 if vt == capi.F64 else torch.float32
+    x = torch.rand(n_col, dtype=tdt, device="cuda")
+    y = torch.empty(n_row, dtype=tdt, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        A.spmv_ex(store, vt, x.data_ptr(), vt, y.data_ptr(), 0, s.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        A.spmv_ex(store, vt, x.data_ptr(), vt, y.data_ptr(), 0, s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def format_sweep(capi, peak):
+    """Every format / store of the configuration, device GB/s."""
+    import torch
+    out = {}
+    n = N_HEADLINE
+    cases = [("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
+             ("CSR_bf16", "CSR", "cqmat", n, 16, 4, capi.BF16, capi.F32),
+             ("ELL_f64", "ELL", "cqmat", n, 16, 1, capi.F64, capi.F64),
+             ("COO_f64", "COO", "cqmat", n, 16, 1, capi.F64, capi.F64),
+             ("SCOO_f64", "SCOO", "cqmat", n, 16, 1, capi.F64, capi.F64),
+             ("DENSE_f64_32768", "DENSE", "cqmat", 32768, 16, 1, capi.F64, capi.F64),
+             ("CSR_f64_cdiag_2^26", "CSR", "cdiag", 1 << 26, 1, 1, capi.F64, capi.F64)]
+    for (key, fmt, gen, nn, c, stores, store, vt) in cases:
+        A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
+        i = A.info()
+        ms = time_product(capi, A, store, vt, i.n_row, i.n_col)
+        vb = {capi.F64: 8, capi.F32: 4, capi.BF16: 2}[store]
+        xb = 8 if vt == capi.F64 else 4
+        if fmt == "CSR":
+            algo = csr_bytes(i.n_row, i.n_col, i.stored, vb, xb)
+        elif fmt == "ELL":
+            algo = i.stored * (vb + 4) + 2 * nn * xb
+        elif fmt in ("COO", "SCOO"):
+            algo = i.stored * (vb + 8) + 2 * nn * xb
+        else:
+            algo = i.stored * vb + 2 * nn * xb
+        gbs = algo / (ms * 1e-3) / 1e9
+        out[key] = {"ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_hbm": round(gbs / peak, 3),
+                    "stored": int(i.stored), "gflops": round(2 * i.stored / (ms * 1e-3) / 1e9, 1)}
+        A.close()
+        torch.cuda.empty_cache()
+    return out
+
+
+def pagerank_bench(capi):
+    """R-MAT 2^24 PageRank to L1 residual 1e-10: FP64 vs FP32/BF16 + FP64 refinement."""
+    import torch
+    t0 = time.time()
+    A = capi.DeviceMatrix.rmat_pagerank(24, 1 << 28, 0.57, 0.19, 0.19, seed=1,
+                                        stores=capi.STORE_F64 | capi.STORE_F32 | capi.STORE_BF16)
+    setup = time.time() - t0
+    info = A.info()
+    n = info.n_row
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    ref = torch.empty(n, dtype=torch.float64, device="cuda")
+    r = A.pagerank(ref.data_ptr(), tol=1e-13, max_iter=2000, precision=capi.F64)
+    res = {"graph": "R-MAT scale 24, 2^28 draws, (0.57,0.19,0.19,0.05), seed 1", "n": n,
+           "edges": int(info.stored), "setup_s": round(setup, 1), "tol": 1e-10,
+           "reference_solve": {"tol": 1e-13, "sweeps": r.iterations, "converged": bool(r.converged)}}
+    times = {}
+    for name, prec in (("fp64", capi.F64), ("fp32_refined", capi.F32), ("bf16_refined", capi.BF16)):
+        A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec)  # warm: workspace + graphs
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            t1 = time.perf_counter()
+            r = A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t1)
+        err = float((out - ref).abs().sum().item())
+        times[name] = min(ts)
+        res[name] = {"ms": round(min(ts) * 1e3, 2), "sweeps": r.iterations, "fp64_sweeps": r.iterations_f64,
+                     "residual": r.residual, "converged": bool(r.converged), "l1_vs_fp64_1e-13": err}
+    res["bf16_over_fp64_time"] = round(times["bf16_refined"] / times["fp64"], 3)
+    res["fp32_over_fp64_time"] = round(times["fp32_refined"] / times["fp64"], 3)
+    A.close()
+    torch.cuda.empty_cache()
+    return res
 
 
 def run_gb300(args, world, rank, local, pg):
@@ -184,6 +271,8 @@ def run_gb300(args, world, rank, local, pg):
     build.build()
     L = capi.lib()
     capi.check(L.tbsla_set_device(local))
+    import torch
+    torch.cuda.set_device(local)
 
     n = N_HEADLINE
     t0 = time.time()
@@ -192,16 +281,12 @@ def run_gb300(args, world, rank, local, pg):
     setup_s = time.time() - t0
     nnz = int(g.values.size)
     algo = csr_bytes(n, n, nnz)
+    kernels = A.info().kernels
 
-    # device vectors and a stream of our own (events are recorded on it)
-    import torch
-    torch.cuda.set_device(local)
     stream = torch.cuda.Stream()
     x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
     y = torch.empty(n, dtype=torch.float64, device="cuda")
     sp = stream.cuda_stream
-    launches_per_step = 2  # csr_merge_kernel + merge_fixup_kernel
-
     with torch.cuda.stream(stream):
         for _ in range(max(args.warmup, 3)):
             A.spmv(x.data_ptr(), y.data_ptr(), 0, sp)
@@ -241,10 +326,11 @@ def run_gb300(args, world, rank, local, pg):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         capi.check(L.tbsla_spmv_host(A.h, hx, n, hy, n, 0))
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_s = max_over_ranks(pg, e2e_s)
+    e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
     L.tbsla_host_free(hx)
     L.tbsla_host_free(hy)
+    A.close()
+    torch.cuda.empty_cache()
 
     if rank != 0:
         return
@@ -253,26 +339,29 @@ def run_gb300(args, world, rank, local, pg):
     achieved = algo / (kern_avg_ms * 1e-3) / 1e9
     threads = os.cpu_count() or 1
     cpu_gbs, cpu_t = cpu_spmv_baseline(g, 5, threads)
+    del g
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "cqmat CSR FP64 SpMV n=2^24 c=16 q=0.1 seed=0", "n": n, "nnz": nnz,
-                   "format": "CSR", "algorithmic_bytes": algo, "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2 (3.56 GB streamed per step)"},
+        "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "format": "CSR", "algorithmic_bytes": algo,
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2: 3.56 GB streamed per step, no flush needed"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES,
-                     "kernel": "csr_merge_kernel", "peak_source": peak_kind,
+                     "kernel": "csr_short_kernel", "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": round(kern_avg_ms, 4)},
-        "hbm_frac_of_measured": round(value / peak, 4),
         "cpu_baseline": {"value": round(cpu_gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": "full matrix, median of 5 products (oracle CSR loop, OpenMP over rows)"},
         "e2e": {"value": round(algo / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
                 "d2h_bytes_per_step": n * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": kernels * args.steps,
         "clocks": clocks,
         "setup_s": round(setup_s, 2),
     }
+    if world == 1 and not args.headline_only:
+        line["formats"] = format_sweep(capi, peak)
+        line["pagerank"] = pagerank_bench(capi)
     print(json.dumps(line), flush=True)
 
 
@@ -282,10 +371,11 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--headline-only", action="store_true", help="skip the format sweep and PageRank")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
-        run_reference(args, world, rank, pg)
+        run_reference(args, world, rank)
     else:
         run_gb300(args, world, rank, local, pg)
     if pg is not None:

@@ -68,6 +68,7 @@ typedef struct {
   int64_t stored;      /* stored entries (ELL: rows*max_col, DENSE: rows*cols) */
   int stores;          /* TBSLA_STORE_* bits present                       */
   int64_t device_bytes;/* device memory held by the handle                 */
+  int kernels;         /* kernel launches of one tbsla_spmv call           */
 } tbsla_matrix_info_t;
 
 /* ---------------------------------------------------------------- misc */

@@ -120,7 +120,7 @@ __device__ __forceinline__ Acc row_sum_thread(const int *__restrict__ colidx, co
 }
 
 // short rows: rows [0, n_rows) when `rows` is NULL, else rows[0..n_rows);
-// grid-stride, so that per-block reductions of an epilogue are amortised
+// grid-stride (one row per thread unless the epilogue caps the grid)
 template <typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ rows, int n_rows,
                                                        const int *__restrict__ rowptr,
@@ -131,8 +131,9 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
   if (!epi.active()) return;
   typename Epi::State es{};
   const uint64_t keep = policy_evict_last();
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_rows; t += gridDim.x * blockDim.x) {
-    const int r = rows ? __ldg(rows + t) : t;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_rows; t += stride) {
+    const int r = rows ? __ldg(rows + t) : (int)t;
     const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
     epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
   }
@@ -166,8 +167,8 @@ __global__ void __launch_bounds__(256) csr_warp_kernel(const int4 *__restrict__ 
   if (!epi.active()) return;
   typename Epi::State es{};
   const uint64_t keep = policy_evict_last();
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
     const int4 it = items[w];
     const Acc s = range_sum_warp<V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
     if ((threadIdx.x & 31) == 0) {
@@ -193,7 +194,7 @@ __global__ void csr_chunk_fixup_kernel(const int2 *__restrict__ huge, int n_huge
     for (int c = first + 1; c < last; ++c) s += partials[c];
     epi.emit(row, s, es);
   }
-  epi.fixup_done(es, n_huge);
+  epi.fixup_done(es, blockIdx.x);
 }
 
 }  // namespace tbsla

@@ -220,7 +220,7 @@ __global__ void csr_huge_fixup_kernel(const int2 *__restrict__ huge_rows, int n_
     for (int c = first + 1; c < last; ++c) s += partials[c];
     epi.emit(row, s, es);
   }
-  epi.fixup_done(es, n_huge);
+  epi.fixup_done(es, blockIdx.x);
 }
 
 }  // namespace tbsla

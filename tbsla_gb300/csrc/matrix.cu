@@ -582,6 +582,20 @@ tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *i
   info->rows = A->rows; info->max_col = A->max_col;
   info->stored = A->stored; info->stores = A->stores;
   info->device_bytes = A->device_bytes;
+  int k = 0;
+  switch (A->format) {
+  case TBSLA_FMT_CSR:
+    if (A->rows > 0 && A->stored > 0) {
+      if (A->csr_variant == 0) k = (A->n_short > 0) + (A->n_warp_items > 0) + (A->n_chunk_rows > 0);
+      else k = 1 + (A->num_huge > 0);
+    }
+    break;
+  case TBSLA_FMT_COO:
+  case TBSLA_FMT_SCOO: k = A->stored > 0 ? 2 : 0; break;
+  case TBSLA_FMT_ELL: k = (A->rows > 0 && A->max_col > 0) ? 1 : 0; break;
+  default: k = (A->rows > 0 && A->cols > 0) ? 1 : 0; break;
+  }
+  info->kernels = k;
   return TBSLA_OK;
 }
 

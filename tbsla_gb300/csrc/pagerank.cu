@@ -79,6 +79,7 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, bool
 // The sweep epilogue: y[row] = beta*v + add (+ r[row]) and the partial sums.
 template <typename YT, typename AccT> struct PrEpi {
   using Acc = AccT;
+  static constexpr bool kReduces = true;  // per-block partials: capped grids
   struct State {
     double a = 0, b = 0, c = 0;
   };
@@ -312,8 +313,8 @@ static tbsla_status_t pr_alloc(void **p, size_t bytes) {
 static int sweep_parts(const tbsla_matrix *A, bool fused) {
   if (!fused) return kAffineBlocks;
   int p = 0;
-  if (A->n_short > 0) p += short_grid(A->n_short);
-  if (A->n_warp_items > 0) p += warp_grid(A->n_warp_items);
+  if (A->n_short > 0) p += short_grid(A->n_short, true);
+  if (A->n_warp_items > 0) p += warp_grid(A->n_warp_items, true);
   if (A->n_chunk_rows > 0) p += fixup_grid(A->n_chunk_rows);
   return std::max(p, 1);
 }

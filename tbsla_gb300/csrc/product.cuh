@@ -18,11 +18,19 @@
 
 namespace tbsla {
 
-// grid of the grid-stride CSR kernels: one pass over the rows, at most
-// kStrideBlocks blocks (each thread then takes several rows)
+// grids of the grid-stride CSR kernels.  Plain products take one row (one
+// warp item) per thread (warp): the most loads in flight.  Epilogues that
+// reduce per block cap the grid at kStrideBlocks blocks, so that each
+// block's reduction covers many rows and the partials stay few.
 constexpr int kStrideBlocks = 152 * 16;
-inline int short_grid(int n_short) { return std::max(1, std::min((n_short + 255) / 256, kStrideBlocks)); }
-inline int warp_grid(int n_items) { return std::max(1, std::min((n_items + 7) / 8, kStrideBlocks)); }
+inline int short_grid(int n_short, bool reduces) {
+  const int g = (int)(((int64_t)n_short + 255) / 256);
+  return std::max(1, reduces ? std::min(g, kStrideBlocks) : g);
+}
+inline int warp_grid(int n_items, bool reduces) {
+  const int g = (int)(((int64_t)n_items + 7) / 8);
+  return std::max(1, reduces ? std::min(g, kStrideBlocks) : g);
+}
 inline int fixup_grid(int n) { return std::max(1, (n + 127) / 128); }
 
 template <typename Acc> inline Carry<Acc> carry_of(const tbsla_matrix *A);
@@ -63,14 +71,14 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
       int base = 0;
       if (A->n_short > 0) {
         epi.set_part_base(base);
-        base += short_grid(A->n_short);
-        csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short), 256, 0, s>>>(A->short_rows, A->n_short, A->idx0,
-                                                                           A->idx1, vals, x, A->f_col, epi);
+        base += short_grid(A->n_short, Epi::kReduces);
+        csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
+            A->short_rows, A->n_short, A->idx0, A->idx1, vals, x, A->f_col, epi);
       }
       if (A->n_warp_items > 0) {
         epi.set_part_base(base);
-        base += warp_grid(A->n_warp_items);
-        csr_warp_kernel<V, XT, Epi><<<warp_grid(A->n_warp_items), 256, 0, s>>>(
+        base += warp_grid(A->n_warp_items, Epi::kReduces);
+        csr_warp_kernel<V, XT, Epi><<<warp_grid(A->n_warp_items, Epi::kReduces), 256, 0, s>>>(
             A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, chunk_partials_of<Acc>(A), epi);
       }
       kt.stop();

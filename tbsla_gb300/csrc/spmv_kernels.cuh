@@ -31,6 +31,7 @@ template <typename Acc> struct Carry {
 // ------------------------------------------------------------ epilogues
 template <typename YT, typename AccT> struct StoreEpi {
   using Acc = AccT;
+  static constexpr bool kReduces = false;  // no per-block partials
   struct State {};
   YT *y;
   int n_out;   // rows that may be written
@@ -48,6 +49,7 @@ template <typename YT, typename AccT> struct StoreEpi {
 // y = A x + x  (the first half of Matrix::a_axpx_, Matrix.cpp:6-11)
 template <typename AccT> struct AddXEpi {
   using Acc = AccT;
+  static constexpr bool kReduces = false;
   struct State {};
   double *y;
   const double *x;
@@ -178,7 +180,7 @@ __global__ void merge_fixup_kernel(int num_tiles, Carry<typename Epi::Acc> carry
       epi.emit(r, s, es);
     }
   }
-  epi.fixup_done(es, num_tiles);
+  epi.fixup_done(es, blockIdx.x);
 }
 
 // --------------------------------------------------------------- COO
