@@ -42,9 +42,10 @@ N_HEADLINE = 1 << 24
 C_HEADLINE = 16
 Q_HEADLINE = 0.1
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
-WORKLOAD = "cqmat CSR FP64 SpMV n=2^24 c=16 q=0.1 seed=0"
-# DRAM bytes (read + write) of one csr_short_kernel launch on this workload,
-# from the ncu capture summarised in profiles/csr_short_kernel_cqmat_2p24.md
+WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
+# DRAM bytes (read + write) of one csr_short_kernel launch on the 2^24
+# workload, from the ncu capture summarised in
+# profiles/csr_short_kernel_cqmat_2p24.md
 NCU_TRAFFIC_BYTES = None
 
 
@@ -165,12 +166,14 @@ def run_reference(args, world, rank):
     build.build()
     obuild(ref=False)
     threads = os.cpu_count() or 1
-    g = capi.generate("CSR", "cqmat", N_HEADLINE, N_HEADLINE, C_HEADLINE, Q_HEADLINE, 0)
+    n = 1 << args.log2n
+    g = capi.generate("CSR", "cqmat", n, n, C_HEADLINE, Q_HEADLINE, 0)
     gbs, t = cpu_spmv_baseline(g, max(args.steps, 1), threads)
     line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n": N_HEADLINE, "nnz": int(g.values.size), "format": "CSR"},
+            "config": {"workload": WORKLOAD.format(log2n=args.log2n), "n": n, "nnz": int(g.values.size),
+                       "format": "CSR"},
             "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                              "sample": f"full matrix, median of {max(args.steps, 1)} products"},
             "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -274,7 +277,7 @@ def run_gb300(args, world, rank, local, pg):
     import torch
     torch.cuda.set_device(local)
 
-    n = N_HEADLINE
+    n = 1 << args.log2n
     t0 = time.time()
     g = capi.generate("CSR", "cqmat", n, n, C_HEADLINE, Q_HEADLINE, 0)
     A = capi.DeviceMatrix.from_generated(g)
@@ -344,11 +347,13 @@ def run_gb300(args, world, rank, local, pg):
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "format": "CSR", "algorithmic_bytes": algo,
+        "config": {"workload": WORKLOAD.format(log2n=args.log2n), "n": n, "nnz": nnz, "format": "CSR",
+                   "algorithmic_bytes": algo,
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: 3.56 GB streamed per step, no flush needed"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES,
+                     "frac": round(achieved / peak, 4),
+                     "traffic": NCU_TRAFFIC_BYTES if args.log2n == 24 else None,
                      "kernel": "csr_short_kernel", "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": round(kern_avg_ms, 4)},
         "cpu_baseline": {"value": round(cpu_gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
@@ -372,8 +377,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--headline-only", action="store_true", help="skip the format sweep and PageRank")
+    ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
+    ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
+    if args.pagerank_only:
+        from tbsla_gb300 import build, capi
+        build.build()
+        print(json.dumps({"pagerank": pagerank_bench(capi)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -121,6 +121,14 @@ tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A);
  * default; 1 = shared-memory row blocks).  Results agree within the FP64
  * bound of the parity tests; the choice only changes speed. */
 tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
+
+/* Tunable knobs of a handle's kernels (what the autotuner sets); results do
+ * not depend on them.
+ *   TBSLA_TUNE_X_L2_KEEP  fraction in [0, 1] of the gathered vector x that the
+ *                         CSR product loads with L2 evict-last priority (the
+ *                         rest with normal priority); default 0.6. */
+typedef enum { TBSLA_TUNE_X_L2_KEEP = 0 } tbsla_tune_knob_t;
+tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
 
 /* --------------------------------------------------------------- SpMV */

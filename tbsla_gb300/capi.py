@@ -21,6 +21,7 @@ FMT_NAME = {v: k for k, v in FMT.items()}
 F64, F32, BF16 = 0, 1, 2
 STORE_F64, STORE_F32, STORE_BF16 = 1, 2, 4
 PR_REFERENCE, PR_DANGLING = 0, 1
+TUNE_X_L2_KEEP = 0
 GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -75,6 +76,7 @@ def lib() -> C.CDLL:
         "tbsla_dense_create": ([C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.POINTER(P)], st),
         "tbsla_matrix_destroy": ([P], st),
         "tbsla_matrix_set_variant": ([P, C.c_int], st),
+        "tbsla_matrix_tune": ([P, C.c_int, C.c_double], st),
         "tbsla_matrix_info": ([P, C.POINTER(MatrixInfo)], st),
         "tbsla_spmv": ([P, _vp, _vp, C.c_int, _vp], st),
         "tbsla_spmv_ex": ([P, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp], st),
@@ -317,6 +319,9 @@ class DeviceMatrix:
         check(lib().tbsla_personalized_pagerank_host(self.h, C.byref(p), _ptr(nd), nd.size, _ptr(out),
                                                      out.size, C.byref(r)))
         return out[:n], r
+
+    def tune(self, knob: int, value: float):
+        check(lib().tbsla_matrix_tune(self.h, knob, float(value)))
 
     def set_variant(self, variant: int):
         check(lib().tbsla_matrix_set_variant(self.h, variant))

@@ -77,6 +77,9 @@ struct tbsla_matrix {
 
   // CSR kernel variant: 0 = direct (row bins), 1 = row blocks
   int csr_variant = 0;
+  // fraction of the gathered vector's lines loaded with L2 evict-last
+  // priority by the direct CSR kernels (tbsla_matrix_tune)
+  float x_keep = 0.6f;
   // CSR direct bins (csr_direct.cuh): short rows (NULL = all rows), warp
   // items (long rows and chunks of huge rows), huge rows, chunk partials
   int *short_rows = nullptr;
@@ -171,6 +174,21 @@ template <> __device__ __forceinline__ __nv_bfloat16 ld_stream(const __nv_bfloat
 __device__ __forceinline__ uint64_t policy_evict_last() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// evict-last for a fraction f of the lines it touches (the others keep their
+// priority); f <= 0 gives normal priority throughout.  Used on the gathered
+// vector: when x is about as large as L2, protecting all of it leaves no room
+// for the streamed matrix lines, which are then fetched again.
+__device__ __forceinline__ uint64_t policy_keep(float f) {
+  uint64_t p;
+  if (f >= 1.f)
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  else if (f > 0.f)
+    asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_unchanged.b64 %0, %1;" : "=l"(p) : "f"(f));
+  else
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
 

@@ -126,11 +126,12 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
                                                        const int *__restrict__ rowptr,
                                                        const int *__restrict__ colidx,
                                                        const V *__restrict__ values,
-                                                       const XT *__restrict__ x, int f_col, Epi epi) {
+                                                       const XT *__restrict__ x, int f_col, float x_keep,
+                                                       Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   typename Epi::State es{};
-  const uint64_t keep = policy_evict_last();
+  const uint64_t keep = policy_keep(x_keep);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_rows; t += stride) {
     const int r = rows ? __ldg(rows + t) : (int)t;
@@ -161,12 +162,12 @@ template <typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_warp_kernel(const int4 *__restrict__ items, int n_items,
                                                       const int *__restrict__ colidx,
                                                       const V *__restrict__ values,
-                                                      const XT *__restrict__ x, int f_col,
+                                                      const XT *__restrict__ x, int f_col, float x_keep,
                                                       typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   typename Epi::State es{};
-  const uint64_t keep = policy_evict_last();
+  const uint64_t keep = policy_keep(x_keep);
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
     const int4 it = items[w];

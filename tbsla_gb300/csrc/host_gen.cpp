@@ -415,6 +415,25 @@ tbsla_status_t generate_arrays(int format, int gen, int n_row, int n_col, int c,
   return fail(TBSLA_ERR_INVALID_ARG, "unknown generator %d", gen);
 }
 
+void cqmat_entry_tagged(uint64_t i, uint64_t nr, uint64_t nc, uint64_t c, double q, unsigned int seed_mult,
+                        int64_t &row, int64_t &col, int &tag) {
+  const Entry e = cqmat_entry(i, nr, nc, c, q, seed_mult);
+  const u64 cc = std::min(nc, c);
+  tag = i < cc * std::min(nc - cc + 1, nr) ? 30 : 31;
+  row = e.row;
+  col = e.col;
+}
+
+void cdiag_entry_tagged(int64_t i, int64_t nc, int64_t cd, int64_t &row, int64_t &col, int &tag) {
+  const Entry e = cdiag_entry(i, nc, cd);
+  if (cd == 0) tag = 10;
+  else if (i < std::max(std::min(nc - cd, cd), (i64)0)) tag = 30;
+  else if (i < std::max(cd + 2 * (nc - 2 * cd), (i64)0)) tag = (i % 2 == 0) ? 31 : 32;
+  else tag = 33;
+  row = e.row;
+  col = e.col;
+}
+
 std::vector<double> cqmat_column_sums(int n_row, int n_col, int c, double q, unsigned int seed_mult) {
   return cqmat_colsum(n_row, n_col, c, q, seed_mult);
 }

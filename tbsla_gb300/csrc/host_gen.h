@@ -25,6 +25,13 @@ tbsla_status_t generate_arrays(int format, int gen, int n_row, int n_col, int c,
                                unsigned int seed_mult, int pr, int pc, int NR, int NC,
                                GenArrays &out);
 
+// entry i of the global generators (values_generation.cpp:4-45): row,
+// column and the reference's branch tag (cqmat: 30 full rows, 31 tail rows;
+// cdiag: 10 main diagonal, 30 / 31 / 32 / 33 by band segment)
+void cqmat_entry_tagged(uint64_t i, uint64_t nr, uint64_t nc, uint64_t c, double q, unsigned int seed_mult,
+                        int64_t &row, int64_t &col, int &tag);
+void cdiag_entry_tagged(int64_t i, int64_t nc, int64_t cd, int64_t &row, int64_t &col, int &tag);
+
 // column sums of the global cqmat (values_generation.cpp:47-62)
 std::vector<double> cqmat_column_sums(int n_row, int n_col, int c, double q, unsigned int seed_mult);
 

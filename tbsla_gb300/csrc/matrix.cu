@@ -569,6 +569,18 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant) {
   return TBSLA_OK;
 }
 
+tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
+  TB_CHECK(A, "matrix is NULL");
+  switch (knob) {
+  case TBSLA_TUNE_X_L2_KEEP:
+    TB_CHECK(value >= 0.0 && value <= 1.0, "x L2 keep fraction %g outside [0, 1]", value);
+    A->x_keep = (float)value;
+    return TBSLA_OK;
+  default:
+    return fail(TBSLA_ERR_INVALID_ARG, "unknown tuning knob %d", knob);
+  }
+}
+
 tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A) {
   free_handle(A);
   return TBSLA_OK;

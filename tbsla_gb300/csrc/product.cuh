@@ -73,13 +73,13 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
         epi.set_part_base(base);
         base += short_grid(A->n_short, Epi::kReduces);
         csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
-            A->short_rows, A->n_short, A->idx0, A->idx1, vals, x, A->f_col, epi);
+            A->short_rows, A->n_short, A->idx0, A->idx1, vals, x, A->f_col, A->x_keep, epi);
       }
       if (A->n_warp_items > 0) {
         epi.set_part_base(base);
         base += warp_grid(A->n_warp_items, Epi::kReduces);
         csr_warp_kernel<V, XT, Epi><<<warp_grid(A->n_warp_items, Epi::kReduces), 256, 0, s>>>(
-            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, chunk_partials_of<Acc>(A), epi);
+            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, A->x_keep, chunk_partials_of<Acc>(A), epi);
       }
       kt.stop();
       if (A->n_chunk_rows > 0) {
