@@ -233,11 +233,12 @@ def format_sweep(capi, peak):
     return out
 
 
-def pagerank_bench(capi):
-    """R-MAT 2^24 PageRank to L1 residual 1e-10: FP64 vs FP32/BF16 + FP64 refinement."""
+def pagerank_bench(capi, scale=24):
+    """R-MAT 2^scale (16 draws per vertex) PageRank to L1 residual 1e-10:
+    FP64 vs FP32/BF16 + FP64 refinement."""
     import torch
     t0 = time.time()
-    A = capi.DeviceMatrix.rmat_pagerank(24, 1 << 28, 0.57, 0.19, 0.19, seed=1,
+    A = capi.DeviceMatrix.rmat_pagerank(scale, 16 << scale, 0.57, 0.19, 0.19, seed=1,
                                         stores=capi.STORE_F64 | capi.STORE_F32 | capi.STORE_BF16)
     setup = time.time() - t0
     info = A.info()
@@ -245,7 +246,7 @@ def pagerank_bench(capi):
     out = torch.empty(n, dtype=torch.float64, device="cuda")
     ref = torch.empty(n, dtype=torch.float64, device="cuda")
     r = A.pagerank(ref.data_ptr(), tol=1e-13, max_iter=2000, precision=capi.F64)
-    res = {"graph": "R-MAT scale 24, 2^28 draws, (0.57,0.19,0.19,0.05), seed 1", "n": n,
+    res = {"graph": f"R-MAT scale {scale}, 2^{scale + 4} draws, (0.57,0.19,0.19,0.05), seed 1", "n": n,
            "edges": int(info.stored), "setup_s": round(setup, 1), "tol": 1e-10,
            "reference_solve": {"tol": 1e-13, "sweeps": r.iterations, "converged": bool(r.converged)}}
     times = {}
@@ -379,12 +380,13 @@ def main():
     ap.add_argument("--headline-only", action="store_true", help="skip the format sweep and PageRank")
     ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
+    ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
     if args.pagerank_only:
         from tbsla_gb300 import build, capi
         build.build()
-        print(json.dumps({"pagerank": pagerank_bench(capi)}), flush=True)
+        print(json.dumps({"pagerank": pagerank_bench(capi, args.rmat_scale)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -126,8 +126,15 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  * not depend on them.
  *   TBSLA_TUNE_X_L2_KEEP  fraction in [0, 1] of the gathered vector x that the
  *                         CSR product loads with L2 evict-last priority (the
- *                         rest with normal priority); default 0.6. */
-typedef enum { TBSLA_TUNE_X_L2_KEEP = 0 } tbsla_tune_knob_t;
+ *                         rest with normal priority); default 0.6.
+ *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
+ *                         decreasing out-degree order (built on first use,
+ *                         kept with the handle): 1 on, 0 off, -1 (default)
+ *                         when the graph is square, has at least 2^20
+ *                         vertices, is not banded and its top tenth of
+ *                         vertices holds half of the entries.  Results are
+ *                         returned in the original labels. */
+typedef enum { TBSLA_TUNE_X_L2_KEEP = 0, TBSLA_TUNE_PR_RELABEL = 1 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
 

@@ -86,6 +86,7 @@ struct tbsla_matrix {
   int n_short = 0;
   int4 *warp_items = nullptr;
   int n_warp_items = 0;
+  int item_class_start[5] = {0, 0, 0, 0, 0};  // items of length class c: [start[c], start[c+1])
   int2 *chunk_rows = nullptr;
   int n_chunk_rows = 0;
   double *chunk_partials = nullptr;
@@ -115,6 +116,15 @@ struct tbsla_matrix {
   void (*pr_work_free)(void *) = nullptr;
   unsigned char *dangling = nullptr;
   double *pr_scratch = nullptr;
+  // PageRank on a relabelled copy (pr_relabel.cu): vertices in decreasing
+  // out-degree order, so that the hot entries of the gathered iterate share
+  // cache lines
+  int pr_relabel_mode = -1;          // tbsla_matrix_tune: -1 auto, 0 off, 1 on
+  int pr_relabel_state = 0;          // 0 undecided, 1 built, 2 declined
+  tbsla_matrix *pr_relabel = nullptr;
+  int *pr_newid = nullptr;           // new label of each vertex (device)
+  std::vector<int> pr_newid_host;    // the same on the host (node lists)
+  double *pr_out = nullptr;          // result in the original labels (device)
 
   // host-path staging
   cudaStream_t stream = nullptr;

@@ -9,13 +9,19 @@
 //     barrier are involved.  The row is summed in
 //     its stored order with one FMA per nonzero (the order of
 //     MatrixCSR::Ax, src/cpp/matrix/MatrixCSR.cpp:133-139).
-//   long (<= kChunk): one warp per row, lanes striding the row, partial sums
-//     combined with a fixed shuffle tree.
-//   huge (> kChunk): the row is cut into chunks of kChunk nonzeros, one warp
+//   long (<= kChunk): a group of L lanes per row, L = 4, 8, 16 or 32 by
+//     length class (kGroupLimit), lanes striding the row, partial sums
+//     combined with a fixed shuffle tree inside the group.
+//   huge (> kChunk): the row is cut into chunks of kChunk nonzeros, 32 lanes
 //     per chunk writing a partial; csr_chunk_fixup_kernel adds the partials of
 //     each row in chunk order.
+// The groups exist for the FP64 pipe (2 lane-operations per clock per SM on
+// GB300; a warp instruction costs the same with 1 or 32 lanes active): one
+// warp per row would spend ~10 FP64 warp instructions per row on its
+// reduction and epilogue, more than the products of a 100-entry row.
 // Row data is read through L1 with the default cache policy, the gathered x
-// evict-last in L2, y written with streaming stores.  No atomics: results do not depend on scheduling.
+// with a fractional evict-last L2 policy, y written with streaming stores.
+// No atomics: results do not depend on scheduling.
 #pragma once
 
 #include <type_traits>
@@ -26,6 +32,11 @@ namespace tbsla {
 
 constexpr int kShortRow = 32;
 constexpr int kChunk = 8192;
+// length classes of the long rows: class c takes rows of at most
+// kGroupLimit[c] entries with kGroupLanes[c] lanes each (chunks: class 3)
+constexpr int kGroupClasses = 4;
+constexpr int kGroupLimit[kGroupClasses] = {96, 256, 1024, kChunk};
+constexpr int kGroupLanes[kGroupClasses] = {4, 8, 16, 32};
 
 __device__ __forceinline__ float bf16_lo(unsigned w) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w & 0xffffu))); }
 __device__ __forceinline__ float bf16_hi(unsigned w) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w >> 16))); }
@@ -141,38 +152,45 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
   epi.block_done(es, blockIdx.x);
 }
 
-// sum of entries [a, b) by one warp: lanes stride the range, fixed shuffle tree
-template <typename V, typename XT, typename Acc>
-__device__ __forceinline__ Acc range_sum_warp(const int *__restrict__ colidx, const V *__restrict__ values,
-                                              const XT *__restrict__ x, int f_col, int a, int b,
-                                              uint64_t keep) {
-  const int lane = threadIdx.x & 31;
+// sum of entries [a, b) by a group of L lanes of one warp (L a power of two
+// <= 32, groups aligned in the warp): lanes stride the range, fixed shuffle
+// tree within the group.  Valid in the group's first lane.
+template <int L, typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc range_sum_group(const int *__restrict__ colidx, const V *__restrict__ values,
+                                               const XT *__restrict__ x, int f_col, int a, int b, uint64_t keep) {
+  const int lane = threadIdx.x & (L - 1);
+  const unsigned mask = L == 32 ? 0xffffffffu : ((1u << (L & 31)) - 1u) << ((threadIdx.x & 31) & ~(L - 1));
   Acc acc = 0;
   #pragma unroll 4
-  for (int k = a + lane; k < b; k += 32)
+  for (int k = a + lane; k < b; k += L)
     acc = fma_acc(to_acc(ld_stream(values + k), Acc()), to_acc(ld_keep(x + (ld_stream(colidx + k) - f_col), keep), Acc()), acc);
   #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  return acc;  // valid in lane 0
+  for (int o = L / 2; o > 0; o >>= 1) acc += __shfl_down_sync(mask, acc, o, L);
+  return acc;
 }
 
-// long rows (one warp each) and chunks of huge rows (one warp each):
-// items[w] = (row, begin, end, partial slot or -1)
-template <typename V, typename XT, typename Epi>
-__global__ void __launch_bounds__(256) csr_warp_kernel(const int4 *__restrict__ items, int n_items,
-                                                      const int *__restrict__ colidx,
-                                                      const V *__restrict__ values,
-                                                      const XT *__restrict__ x, int f_col, float x_keep,
-                                                      typename Epi::Acc *__restrict__ partials, Epi epi) {
+// Rows longer than kShortRow and chunks of huge rows, L lanes per item:
+// items[i] = (row, begin, end, partial slot or -1).  A warp holds 32/L
+// groups, so its FP64 reduction steps and the epilogue serve 32/L rows at
+// once (every FP64 warp instruction costs the same on this part whatever
+// its active lanes).  Items come in length classes, so the groups of a warp
+// take similar trip counts.
+template <int L, typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_group_kernel(const int4 *__restrict__ items, int n_items,
+                                                       const int *__restrict__ colidx,
+                                                       const V *__restrict__ values,
+                                                       const XT *__restrict__ x, int f_col, float x_keep,
+                                                       typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   typename Epi::State es{};
   const uint64_t keep = policy_keep(x_keep);
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
-    const int4 it = items[w];
-    const Acc s = range_sum_warp<V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
-    if ((threadIdx.x & 31) == 0) {
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / L;
+  // every lane of a group sees the same item sequence (same trip count)
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L; g < n_items; g += ng) {
+    const int4 it = items[g];
+    const Acc s = range_sum_group<L, V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
+    if ((threadIdx.x & (L - 1)) == 0) {
       if (it.w < 0) epi.emit(it.x, s, es);
       else partials[it.w] = s;
     }

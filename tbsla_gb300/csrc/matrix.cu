@@ -172,12 +172,13 @@ static void free_handle(tbsla_matrix *A) {
   if (!A) return;
   cudaSetDevice(A->device);
   if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
+  if (A->pr_relabel) free_handle(A->pr_relabel);
   for (void *p : A->values) if (p) cudaFree(p);
   void *ptrs[] = {A->idx0, A->idx1, A->row_blocks, A->huge_rows, A->huge_partials, A->huge_partials32,
                   A->short_rows, A->warp_items, A->chunk_rows, A->chunk_partials, A->chunk_partials32,
                   A->tile_start, A->tile_head_row, A->tile_head_val,
                   A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
-                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err};
+                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err, A->pr_newid, A->pr_out};
   for (void *p : ptrs) if (p) cudaFree(p);
   if (A->stream) cudaStreamDestroy(A->stream);
   for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -350,7 +351,7 @@ static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *c
   // direct bins: short rows by thread, long rows by warp, huge rows by chunk
   {
     std::vector<int> shorts;
-    std::vector<int4> items;
+    std::vector<int4> cls[kGroupClasses];
     std::vector<int2> chunk_rows;
     int slot = 0;
     bool all_short = true;
@@ -358,10 +359,22 @@ static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *c
       const int len = rp[r + 1] - rp[r];
       if (len <= kShortRow) { shorts.push_back(r); continue; }
       all_short = false;
-      if (len <= kChunk) { items.push_back(make_int4(r, rp[r], rp[r + 1], -1)); continue; }
+      if (len <= kChunk) {
+        int c = 0;
+        while (len > kGroupLimit[c]) ++c;
+        cls[c].push_back(make_int4(r, rp[r], rp[r + 1], -1));
+        continue;
+      }
       chunk_rows.push_back(make_int2(r, slot));
-      for (int c = rp[r]; c < rp[r + 1]; c += kChunk) items.push_back(make_int4(r, c, std::min(c + kChunk, rp[r + 1]), slot++));
+      for (int c = rp[r]; c < rp[r + 1]; c += kChunk)
+        cls[kGroupClasses - 1].push_back(make_int4(r, c, std::min(c + kChunk, rp[r + 1]), slot++));
     }
+    std::vector<int4> items;
+    for (int c = 0; c < kGroupClasses; ++c) {
+      A->item_class_start[c] = (int)items.size();
+      items.insert(items.end(), cls[c].begin(), cls[c].end());
+    }
+    A->item_class_start[kGroupClasses] = (int)items.size();
     A->n_short = (int)shorts.size();
     if (!all_short && !shorts.empty()) {
       TB_TRY(alloc_n(A, &A->short_rows, (int64_t)shorts.size()));
@@ -575,6 +588,11 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
   case TBSLA_TUNE_X_L2_KEEP:
     TB_CHECK(value >= 0.0 && value <= 1.0, "x L2 keep fraction %g outside [0, 1]", value);
     A->x_keep = (float)value;
+    if (A->pr_relabel) A->pr_relabel->x_keep = (float)value;
+    return TBSLA_OK;
+  case TBSLA_TUNE_PR_RELABEL:
+    TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0, "PageRank relabel mode %g not -1, 0 or 1", value);
+    A->pr_relabel_mode = (int)value;
     return TBSLA_OK;
   default:
     return fail(TBSLA_ERR_INVALID_ARG, "unknown tuning knob %d", knob);
@@ -598,7 +616,10 @@ tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *i
   switch (A->format) {
   case TBSLA_FMT_CSR:
     if (A->rows > 0 && A->stored > 0) {
-      if (A->csr_variant == 0) k = (A->n_short > 0) + (A->n_warp_items > 0) + (A->n_chunk_rows > 0);
+      if (A->csr_variant == 0) {
+        k = (A->n_short > 0) + (A->n_chunk_rows > 0);
+        for (int c = 0; c < kGroupClasses; ++c) k += A->item_class_start[c + 1] > A->item_class_start[c];
+      }
       else k = 1 + (A->num_huge > 0);
     }
     break;

@@ -314,7 +314,10 @@ static int sweep_parts(const tbsla_matrix *A, bool fused) {
   if (!fused) return kAffineBlocks;
   int p = 0;
   if (A->n_short > 0) p += short_grid(A->n_short, true);
-  if (A->n_warp_items > 0) p += warp_grid(A->n_warp_items, true);
+  for (int c = 0; c < kGroupClasses; ++c) {
+    const int count = A->item_class_start[c + 1] - A->item_class_start[c];
+    if (count > 0) p += group_grid(count, kGroupLanes[c], true);
+  }
   if (A->n_chunk_rows > 0) p += fixup_grid(A->n_chunk_rows);
   return std::max(p, 1);
 }
@@ -509,6 +512,9 @@ static tbsla_status_t run_f64(tbsla_matrix *A, PrWork *W, int mode, bool with_tm
 
 static double *pr_result(PrWork *W) { return W->result; }
 
+tbsla_status_t pr_relabelled(tbsla_matrix *A, tbsla_matrix **B);
+tbsla_status_t pr_relabel_gather(const tbsla_matrix *A, const double *x, double *out, cudaStream_t s);
+
 }  // namespace tbsla
 
 using namespace tbsla;
@@ -642,11 +648,46 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   return TBSLA_OK;
 }
 
+// PageRank of A, on its relabelled copy when there is one (pr_relabel.cu);
+// *result points to the vector in A's labels (d_out, or a buffer of A's)
+static tbsla_status_t pagerank_entry(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const int *nodes,
+                                     int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user,
+                                     const double **result) {
+  TB_CHECK(A && p, "NULL argument");
+  TB_CUDA(cudaSetDevice(A->device));
+  tbsla_matrix *B = nullptr;
+  TB_TRY(pr_relabelled(A, &B));
+  if (!B) {
+    TB_TRY(pagerank_impl(A, p, nodes, n_nodes, d_out, res, user));
+    if (result) *result = d_out ? d_out : pr_result(static_cast<PrWork *>(A->pr_work));
+    return TBSLA_OK;
+  }
+  const int n = A->n_row;
+  std::vector<int> mapped;
+  if (nodes) {
+    mapped.resize((size_t)std::max(n_nodes, 0));
+    for (int k = 0; k < n_nodes; ++k)
+      mapped[(size_t)k] = nodes[k] >= 0 && nodes[k] < n ? A->pr_newid_host[(size_t)nodes[k]] : -1;
+  }
+  TB_TRY(pagerank_impl(B, p, nodes ? mapped.data() : nullptr, n_nodes, nullptr, res, user));
+  PrWork *W = static_cast<PrWork *>(B->pr_work);
+  double *out = d_out;
+  if (!out) {
+    if (!A->pr_out) TB_TRY(dev_alloc(A, (void **)&A->pr_out, (size_t)n * sizeof(double)));
+    out = A->pr_out;
+  }
+  TB_TRY(pr_relabel_gather(A, pr_result(W), out, W->stream));
+  TB_CUDA(cudaStreamSynchronize(W->stream));
+  if (result) *result = out;
+  return TBSLA_OK;
+}
+
 extern "C" {
 
 tbsla_status_t tbsla_pagerank(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, double *d_out,
                               tbsla_pagerank_result_t *result, void *stream) {
-  return pagerank_impl(const_cast<tbsla_matrix *>(A), p, nullptr, 0, d_out, result, (cudaStream_t)stream);
+  return pagerank_entry(const_cast<tbsla_matrix *>(A), p, nullptr, 0, d_out, result, (cudaStream_t)stream,
+                        nullptr);
 }
 
 tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, double *out,
@@ -654,9 +695,9 @@ tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_param
   TB_CHECK(A && out, "NULL argument");
   TB_CHECK(n_out >= A->n_col, "output has %lld entries, need %d", (long long)n_out, A->n_col);
   std::lock_guard<std::mutex> lk(A->host_mu);
-  TB_TRY(pagerank_impl(A, p, nullptr, 0, nullptr, result, nullptr));
-  PrWork *W = static_cast<PrWork *>(A->pr_work);
-  TB_CUDA(cudaMemcpy(out, pr_result(W), (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
+  const double *r = nullptr;
+  TB_TRY(pagerank_entry(A, p, nullptr, 0, nullptr, result, nullptr, &r));
+  TB_CUDA(cudaMemcpy(out, r, (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
   return TBSLA_OK;
 }
 
@@ -669,9 +710,9 @@ tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_p
   tbsla_pagerank_params_t q = *p;
   q.mode = TBSLA_PR_REFERENCE;
   q.precision = TBSLA_F64;
-  TB_TRY(pagerank_impl(A, &q, nodes, n_nodes, nullptr, result, nullptr));
-  PrWork *W = static_cast<PrWork *>(A->pr_work);
-  TB_CUDA(cudaMemcpy(out, pr_result(W), (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
+  const double *r = nullptr;
+  TB_TRY(pagerank_entry(A, &q, nodes, n_nodes, nullptr, result, nullptr, &r));
+  TB_CUDA(cudaMemcpy(out, r, (size_t)A->n_col * 8, cudaMemcpyDeviceToHost));
   return TBSLA_OK;
 }
 

@@ -27,8 +27,9 @@ inline int short_grid(int n_short, bool reduces) {
   const int g = (int)(((int64_t)n_short + 255) / 256);
   return std::max(1, reduces ? std::min(g, kStrideBlocks) : g);
 }
-inline int warp_grid(int n_items, bool reduces) {
-  const int g = (int)(((int64_t)n_items + 7) / 8);
+inline int group_grid(int n_items, int lanes, bool reduces) {
+  const int per_block = 256 / lanes;
+  const int g = (int)(((int64_t)n_items + per_block - 1) / per_block);
   return std::max(1, reduces ? std::min(g, kStrideBlocks) : g);
 }
 inline int fixup_grid(int n) { return std::max(1, (n + 127) / 128); }
@@ -75,11 +76,28 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
         csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
             A->short_rows, A->n_short, A->idx0, A->idx1, vals, x, A->f_col, A->x_keep, epi);
       }
-      if (A->n_warp_items > 0) {
+      for (int c = 0; c < kGroupClasses; ++c) {
+        const int first = A->item_class_start[c], count = A->item_class_start[c + 1] - first;
+        if (count == 0) continue;
+        const int grid = group_grid(count, kGroupLanes[c], Epi::kReduces);
         epi.set_part_base(base);
-        base += warp_grid(A->n_warp_items, Epi::kReduces);
-        csr_warp_kernel<V, XT, Epi><<<warp_grid(A->n_warp_items, Epi::kReduces), 256, 0, s>>>(
-            A->warp_items, A->n_warp_items, A->idx1, vals, x, A->f_col, A->x_keep, chunk_partials_of<Acc>(A), epi);
+        base += grid;
+        const int4 *items = A->warp_items + first;
+        Acc *parts = chunk_partials_of<Acc>(A);
+        switch (kGroupLanes[c]) {
+        case 4:
+          csr_group_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
+          break;
+        case 8:
+          csr_group_kernel<8, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
+          break;
+        case 16:
+          csr_group_kernel<16, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
+          break;
+        default:
+          csr_group_kernel<32, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
+          break;
+        }
       }
       kt.stop();
       if (A->n_chunk_rows > 0) {

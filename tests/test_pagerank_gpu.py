@@ -104,6 +104,34 @@ def test_dangling_mode_fp64_and_mixed(gpu, orc, scale):
         assert err < 1e-10, (prec, err, r.iterations, r.iterations_f64)
 
 
+@pytest.mark.parametrize("scale,mode", [(14, 1), (20, -1)])
+def test_relabelled_pagerank(gpu, orc, scale, mode):
+    """PageRank on the degree-relabelled copy (forced at scale 14, chosen by
+    the automatic rule at 2^20) returns the vector of the original labels."""
+    m = 16 << scale
+    A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=3, stores=gpu.STORE_F64 | gpu.STORE_BF16)
+    P = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=3, stores=gpu.STORE_F64 | gpu.STORE_BF16)
+    P.tune(gpu.TUNE_PR_RELABEL, 0)
+    A.tune(gpu.TUNE_PR_RELABEL, mode)
+    rp, ci, va, dang = rmat_csr_oracle(orc, scale, m, 3)
+    xo, _, res_o = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 1e-14, 5000, threads=8)
+    xo = xo / math.fsum(xo)
+    for prec in (gpu.F64, gpu.BF16):
+        x, r = A.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
+        xp, rp_ = P.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
+        assert r.converged and rp_.converged
+        assert np.abs(x - xo).sum() < 1e-10, prec
+        assert np.abs(x - xp).sum() < 1e-10, prec
+    # reference mode and a personalised node list (labels mapped inside)
+    x, r = A.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
+    xp, rp_ = P.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
+    assert abs(r.iterations - rp_.iterations) <= 1 and np.abs(x - xp).sum() < 1e-8
+    nodes = [0, 7, 7, (1 << scale) - 1, 12345 % (1 << scale)]
+    y, r = A.personalized_pagerank_host(nodes, tol=1e-9, max_iter=500)
+    yp, rp_ = P.personalized_pagerank_host(nodes, tol=1e-9, max_iter=500)
+    assert abs(r.iterations - rp_.iterations) <= 1 and np.abs(y - yp).sum() < 1e-8
+
+
 def test_pagerank_argument_checks(gpu):
     g = gpu.generate("CSR", "cqmat_stochastic", 50, 40, 5, 0.1, 0)
     m = gpu.DeviceMatrix.from_generated(g)
