@@ -160,6 +160,28 @@ tbsla_status_t tbsla_spmv_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
 tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *y,
                                int64_t ny, int vect_incr);
 
+/* y = A^T x (CSR handles): the gradient of y = A x with respect to x.  x has
+ * n_row entries, y n_col entries (indexed col - f_col).  The transpose is
+ * built on the first call (host sort of the entries by column, stable) and
+ * kept with the handle; store / types as tbsla_spmv_ex.  No reference
+ * counterpart. */
+tbsla_status_t tbsla_spmv_transpose_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_dtype_t x_type,
+                                       const void *d_x, tbsla_dtype_t y_type, void *d_y, void *stream);
+
+/* out[k] = scale * a[row(k)] * b[col(k) - f_col] for every stored entry k of
+ * a CSR handle, in its entry order: the gradient of y = A x with respect to
+ * the values (a = dL/dy, b = x, scale = 1).  a, b and out are FP64 for
+ * type TBSLA_F64, FP32 for TBSLA_F32.  No reference counterpart. */
+tbsla_status_t tbsla_csr_grad_values(const tbsla_matrix_t *A, tbsla_dtype_t type, const void *d_a,
+                                     const void *d_b, double scale, void *d_out, void *stream);
+
+/* Replaces the values of a CSR handle (entry order of its creation arrays,
+ * nnz entries of `type` on the device) and re-derives its reduced-precision
+ * stores; the transposed copy follows and cached PageRank state is rebuilt
+ * on next use.  No reference counterpart. */
+tbsla_status_t tbsla_matrix_set_values(tbsla_matrix_t *A, tbsla_dtype_t type, const void *d_values,
+                                       void *stream);
+
 /* r = A (A x + x): Matrix::a_axpx_ (Matrix.cpp:6-11), square matrices; the
  * "+ x" is fused into the first product.  d_tmp: n_row doubles of scratch or
  * NULL to use the handle's own. */
@@ -195,7 +217,13 @@ typedef enum {
   /* x0 = 1/n; x = beta*A x + (beta*dangling(x) + (1-beta)*sum(x))/n, where
    * dangling(x) sums x over columns of A with no stored entry; stop when
    * ||x - x_prev||_1 < tol.  Result sums to 1. */
-  TBSLA_PR_DANGLING = 1
+  TBSLA_PR_DANGLING = 1,
+  /* The same fixed point with a teleport vector v (tbsla_pagerank_teleport):
+   * x0 = v; x = beta*A x + (beta*dangling(x) + (1-beta)) v; stop when
+   * ||x - x_prev||_1 < tol.  This is the affine form of TBSLA_PR_DANGLING (for
+   * a column-stochastic A and v = 1/n they agree) and the function that
+   * tbsla_pagerank_adjoint differentiates.  FP64 only; no normalisation. */
+  TBSLA_PR_TELEPORT = 2
 } tbsla_pr_mode_t;
 
 typedef struct {
@@ -224,6 +252,29 @@ tbsla_status_t tbsla_pagerank(const tbsla_matrix_t *A, const tbsla_pagerank_para
                               double *d_out, tbsla_pagerank_result_t *result, void *stream);
 tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
                                    double *out, int64_t n_out, tbsla_pagerank_result_t *result);
+
+/* TBSLA_PR_TELEPORT with the teleport vector d_v (n_col doubles on the
+ * device); p->mode is ignored.  No reference counterpart. */
+tbsla_status_t tbsla_pagerank_teleport(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                       const double *d_v, double *d_out, tbsla_pagerank_result_t *result,
+                                       void *stream);
+
+/* Gradients of L(x*) through the TBSLA_PR_TELEPORT fixed point x* of A
+ * (square CSR).  With d the dangling columns of A and w = dL/dx* (d_w), the
+ * adjoint lambda solves lambda = beta*A^T lambda + beta*d*(v . lambda) + w
+ * (sweeps on the transpose, stopped when ||lambda - lambda_prev||_1 < p->tol
+ * or after p->max_iter sweeps); then
+ *   dL/dvalues[k] = beta * lambda[row(k)] * x*[col(k)]   (d_grad_values, nnz
+ *                   doubles in the handle's entry order; NULL to skip)
+ *   dL/dv         = (beta * d . x* + 1 - beta) * lambda  (d_grad_v, n; NULL
+ *                   to skip)
+ * d_v: the teleport vector of the forward solve (NULL: uniform 1/n); d_x: x*.
+ * The dangling set is structural (columns with no stored entry).  No
+ * reference counterpart. */
+tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                      const double *d_v, const double *d_x, const double *d_w,
+                                      double *d_grad_values, double *d_grad_v,
+                                      tbsla_pagerank_result_t *result, void *stream);
 
 /* Matrix::personalized_page_rank (Matrix.cpp:63-114): as TBSLA_PR_REFERENCE
  * with b0 = 0.25 and the teleport term (1-beta)*sum(b_prev)/n_nodes added only

@@ -146,6 +146,13 @@ class Oracle:
         L.orc_page_rank_dangling.argtypes = [C.c_int, _ip, _ip, _dp, _up, C.c_double, C.c_double,
                                              C.c_int, _dp, C.POINTER(C.c_double), C.c_int]
         L.orc_page_rank_dangling.restype = C.c_int
+        vp = C.c_void_p
+        L.orc_pagerank_teleport.argtypes = [C.c_int, _ip, _ip, _dp, _up, vp, C.c_double, C.c_double, C.c_int,
+                                            _dp, C.POINTER(C.c_double)]
+        L.orc_pagerank_teleport.restype = C.c_int
+        L.orc_pagerank_adjoint.argtypes = [C.c_int, _ip, _ip, _dp, _up, vp, _dp, _dp, C.c_double, C.c_double,
+                                           C.c_int, vp, vp]
+        L.orc_pagerank_adjoint.restype = C.c_int
         L.orc_rmat_edges.argtypes = [C.c_int, C.c_int64, C.c_double, C.c_double, C.c_double,
                                      C.c_uint64, _ip, _ip]
         L.orc_cqmat_sum_columns.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_double, C.c_uint,
@@ -209,6 +216,34 @@ class Oracle:
                                            np.ascontiguousarray(dangling, np.uint8), beta, tol, max_it,
                                            x, C.byref(res), threads)
         return x, it, res.value
+
+    def pagerank_teleport(self, rowptr, colidx, values, dangling, v, beta, tol, max_it):
+        """Affine (teleport) PageRank x = beta A x + (beta d.x + 1 - beta) v; v None = uniform."""
+        n = rowptr.size - 1
+        x = np.empty(n, np.float64)
+        res = C.c_double(0)
+        vv = None if v is None else np.ascontiguousarray(v, np.float64)
+        it = self.L.orc_pagerank_teleport(n, np.ascontiguousarray(rowptr, np.int32),
+                                          np.ascontiguousarray(colidx, np.int32),
+                                          np.ascontiguousarray(values, np.float64),
+                                          np.ascontiguousarray(dangling, np.uint8),
+                                          None if vv is None else vv.ctypes.data, beta, tol, max_it, x, C.byref(res))
+        return x, it, res.value
+
+    def pagerank_adjoint(self, rowptr, colidx, values, dangling, v, x, w, beta, tol, max_it):
+        """Gradients of L(x*) (w = dL/dx*) w.r.t. the values and the teleport vector."""
+        n = rowptr.size - 1
+        gvals = np.empty(values.size, np.float64)
+        gv = np.empty(n, np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, np.float64)
+        it = self.L.orc_pagerank_adjoint(n, np.ascontiguousarray(rowptr, np.int32),
+                                         np.ascontiguousarray(colidx, np.int32),
+                                         np.ascontiguousarray(values, np.float64),
+                                         np.ascontiguousarray(dangling, np.uint8),
+                                         None if vv is None else vv.ctypes.data,
+                                         np.ascontiguousarray(x, np.float64), np.ascontiguousarray(w, np.float64),
+                                         beta, tol, max_it, gvals.ctypes.data, gv.ctypes.data)
+        return gvals, gv, it
 
     def cqmat_sum_columns(self, nr, nc, c, q, seed_mult):
         s = np.zeros(nc, np.float64)

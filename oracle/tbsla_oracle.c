@@ -818,3 +818,76 @@ uint64_t orc_fnv1a(const void *data, size_t nbytes) {
   for (size_t i = 0; i < nbytes; i++) { h ^= p[i]; h *= 1099511628211ull; }
   return h;
 }
+
+/* ------------------------------------------------------------------------ */
+/* PageRank in affine (teleport) form and its adjoint.  No reference         */
+/* counterpart: the fixed point x = beta*A x + (beta*d.x + 1 - beta) v, with */
+/* d the dangling columns, and lambda = beta*A^T lambda + beta*d*(v.lambda) */
+/* + w, the adjoint of L(x*) with w = dL/dx*.  Gradients:                    */
+/*   dL/dA[k] = beta*lambda[row(k)]*x[col(k)],                               */
+/*   dL/dv    = (beta*d.x + 1 - beta)*lambda.                                */
+/* Jacobi sweeps from x0 = v / lambda0 = w; max_it sweeps at most, stop when */
+/* the L1 change is below tol.  v NULL means uniform 1/n.                    */
+/* ------------------------------------------------------------------------ */
+static double tele_v(const double *v, int i, int n) { return v ? v[i] : 1.0 / n; }
+
+int orc_pagerank_teleport(int n, const int *rowptr, const int *colidx, const double *values,
+                          const unsigned char *dangling, const double *v, double beta, double tol,
+                          int max_it, double *x, double *resid) {
+  double *xn = (double *)malloc((n > 0 ? n : 1) * sizeof(double));
+  for (int i = 0; i < n; i++) x[i] = tele_v(v, i, n);
+  int it = 0;
+  double res = INFINITY;
+  while (it < max_it) {
+    double d = 0;
+    for (int j = 0; j < n; j++) if (dangling[j]) d += x[j];
+    const double a = beta * d + (1 - beta);
+    res = 0;
+    for (int i = 0; i < n; i++) {
+      double t = 0;
+      for (int k = rowptr[i]; k < rowptr[i + 1]; k++) t += values[k] * x[colidx[k]];
+      xn[i] = beta * t + a * tele_v(v, i, n);
+      res += fabs(xn[i] - x[i]);
+    }
+    memcpy(x, xn, n * sizeof(double));
+    it++;
+    if (res < tol) break;
+  }
+  free(xn);
+  if (resid) *resid = res;
+  return it;
+}
+
+int orc_pagerank_adjoint(int n, const int *rowptr, const int *colidx, const double *values,
+                         const unsigned char *dangling, const double *v, const double *x, const double *w,
+                         double beta, double tol, int max_it, double *grad_values, double *grad_v) {
+  double *lam = (double *)malloc((n > 0 ? n : 1) * sizeof(double));
+  double *t = (double *)malloc((n > 0 ? n : 1) * sizeof(double));
+  memcpy(lam, w, n * sizeof(double));
+  int it = 0;
+  while (it < max_it) {
+    double vl = 0;
+    for (int j = 0; j < n; j++) vl += tele_v(v, j, n) * lam[j];
+    for (int j = 0; j < n; j++) t[j] = 0;
+    for (int i = 0; i < n; i++)
+      for (int k = rowptr[i]; k < rowptr[i + 1]; k++) t[colidx[k]] += values[k] * lam[i];
+    double res = 0;
+    for (int j = 0; j < n; j++) {
+      const double nl = beta * t[j] + w[j] + (dangling[j] ? beta * vl : 0.0);
+      res += fabs(nl - lam[j]);
+      lam[j] = nl;
+    }
+    it++;
+    if (res < tol) break;
+  }
+  double dx = 0;
+  for (int j = 0; j < n; j++) if (dangling[j]) dx += x[j];
+  if (grad_v)
+    for (int j = 0; j < n; j++) grad_v[j] = (beta * dx + 1 - beta) * lam[j];
+  if (grad_values)
+    for (int i = 0; i < n; i++)
+      for (int k = rowptr[i]; k < rowptr[i + 1]; k++) grad_values[k] = beta * lam[i] * x[colidx[k]];
+  free(lam);
+  free(t);
+  return it;
+}

@@ -92,6 +92,13 @@ int orc_personalized_page_rank(const orc_matrix *m, double epsilon, double beta,
 int orc_page_rank_dangling(int n, const int *rowptr, const int *colidx, const double *values,
                            const unsigned char *dangling, double beta, double tol, int max_it,
                            double *x, double *resid, int threads);
+/* affine (teleport) PageRank and its adjoint; no reference counterpart */
+int orc_pagerank_teleport(int n, const int *rowptr, const int *colidx, const double *values,
+                          const unsigned char *dangling, const double *v, double beta, double tol,
+                          int max_it, double *x, double *resid);
+int orc_pagerank_adjoint(int n, const int *rowptr, const int *colidx, const double *values,
+                         const unsigned char *dangling, const double *v, const double *x, const double *w,
+                         double beta, double tol, int max_it, double *grad_values, double *grad_v);
 
 /* R-MAT edge list (Chakrabarti, Zhan, Faloutsos 2004): recursive quadrant
  * choice per bit with probabilities (a,b,c,1-a-b-c), counter-based uniform

@@ -20,7 +20,7 @@ FMT = {"COO": 0, "SCOO": 1, "CSR": 2, "ELL": 3, "DENSE": 4}
 FMT_NAME = {v: k for k, v in FMT.items()}
 F64, F32, BF16 = 0, 1, 2
 STORE_F64, STORE_F32, STORE_BF16 = 1, 2, 4
-PR_REFERENCE, PR_DANGLING = 0, 1
+PR_REFERENCE, PR_DANGLING, PR_TELEPORT = 0, 1, 2
 TUNE_X_L2_KEEP, TUNE_PR_RELABEL = 0, 1
 GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2}
 
@@ -107,6 +107,12 @@ def lib() -> C.CDLL:
         "tbsla_rmat_pagerank_matrix": ([C.c_int, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_uint64,
                                         C.c_int, C.POINTER(P)], st),
         "tbsla_csr_download": ([P, _vp, _vp, _vp], st),
+        "tbsla_spmv_transpose_ex": ([P, C.c_int, C.c_int, _vp, C.c_int, _vp, _vp], st),
+        "tbsla_csr_grad_values": ([P, C.c_int, _vp, _vp, C.c_double, _vp, _vp], st),
+        "tbsla_matrix_set_values": ([P, C.c_int, _vp, _vp], st),
+        "tbsla_pagerank_teleport": ([P, C.POINTER(PageRankParams), _vp, _vp, C.POINTER(PageRankResult), _vp], st),
+        "tbsla_pagerank_adjoint": ([P, C.POINTER(PageRankParams), _vp, _vp, _vp, _vp, _vp,
+                                    C.POINTER(PageRankResult), _vp], st),
     }
     for name, (args, res) in list(sig.items()) + list(optional.items()):
         if not hasattr(L, name):
@@ -319,6 +325,30 @@ class DeviceMatrix:
         check(lib().tbsla_personalized_pagerank_host(self.h, C.byref(p), _ptr(nd), nd.size, _ptr(out),
                                                      out.size, C.byref(r)))
         return out[:n], r
+
+    # ---- differentiation (device pointers as ints, stream as int or None)
+    def spmv_transpose_ex(self, store: int, x_type: int, d_x: int, y_type: int, d_y: int, stream=None):
+        check(lib().tbsla_spmv_transpose_ex(self.h, store, x_type, d_x, y_type, d_y, stream))
+
+    def grad_values(self, dtype: int, d_a: int, d_b: int, scale: float, d_out: int, stream=None):
+        check(lib().tbsla_csr_grad_values(self.h, dtype, d_a, d_b, float(scale), d_out, stream))
+
+    def set_values(self, dtype: int, d_values: int, stream=None):
+        check(lib().tbsla_matrix_set_values(self.h, dtype, d_values, stream))
+
+    def pagerank_teleport(self, d_v: int, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, stream=None):
+        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0)
+        r = PageRankResult()
+        check(lib().tbsla_pagerank_teleport(self.h, C.byref(p), d_v, d_out, C.byref(r), stream))
+        return r
+
+    def pagerank_adjoint(self, d_v, d_x: int, d_w: int, d_grad_values, d_grad_v, beta=0.85, tol=1e-12,
+                         max_iter=10000, stream=None):
+        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0)
+        r = PageRankResult()
+        check(lib().tbsla_pagerank_adjoint(self.h, C.byref(p), d_v, d_x, d_w, d_grad_values, d_grad_v,
+                                           C.byref(r), stream))
+        return r
 
     def tune(self, knob: int, value: float):
         check(lib().tbsla_matrix_tune(self.h, knob, float(value)))

@@ -125,6 +125,10 @@ struct tbsla_matrix {
   int *pr_newid = nullptr;           // new label of each vertex (device)
   std::vector<int> pr_newid_host;    // the same on the host (node lists)
   double *pr_out = nullptr;          // result in the original labels (device)
+  // transposed copy (transpose.cu), built on first use: entry k' of the copy
+  // holds entry transpose_perm[k'] of this matrix
+  tbsla_matrix *transpose = nullptr;
+  int *transpose_perm = nullptr;
 
   // host-path staging
   cudaStream_t stream = nullptr;

@@ -109,6 +109,11 @@ __global__ void f64_to_bf16_kernel(const double *in, __nv_bfloat16 *out, int64_t
     out[i] = __double2bfloat16(in[i]);
 }
 
+__global__ void f32_to_f64_kernel(const float *in, double *out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+
 static int grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32);
@@ -146,6 +151,20 @@ static tbsla_status_t upload_values(tbsla_matrix *A, const double *host, int64_t
   return TBSLA_OK;
 }
 
+// The F32 / BF16 stores of A recomputed from its F64 store
+tbsla_status_t rederive_stores(tbsla_matrix *A, cudaStream_t s) {
+  const int64_t n = A->format == TBSLA_FMT_ELL ? (int64_t)A->rows_pad * A->max_col : A->stored;
+  if (!A->values[0] || n == 0) return TBSLA_OK;
+  const double *v = static_cast<const double *>(A->values[0]);
+  if (A->values[1]) f64_to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(v, static_cast<float *>(A->values[1]), n);
+  if (A->values[2])
+    f64_to_bf16_kernel<<<grid_for(n, 256), 256, 0, s>>>(v, static_cast<__nv_bfloat16 *>(A->values[2]), n);
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+tbsla_status_t transpose_refresh(tbsla_matrix *A, cudaStream_t s);
+
 static tbsla_status_t alloc_carries(tbsla_matrix *A) {
   const int nt = std::max(A->num_tiles, 1);
   TB_TRY(alloc_n(A, &A->tile_head_row, nt));
@@ -173,12 +192,14 @@ static void free_handle(tbsla_matrix *A) {
   cudaSetDevice(A->device);
   if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
   if (A->pr_relabel) free_handle(A->pr_relabel);
+  if (A->transpose) free_handle(A->transpose);
   for (void *p : A->values) if (p) cudaFree(p);
   void *ptrs[] = {A->idx0, A->idx1, A->row_blocks, A->huge_rows, A->huge_partials, A->huge_partials32,
                   A->short_rows, A->warp_items, A->chunk_rows, A->chunk_partials, A->chunk_partials32,
                   A->tile_start, A->tile_head_row, A->tile_head_val,
                   A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
-                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err, A->pr_newid, A->pr_out};
+                  A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err, A->pr_newid, A->pr_out,
+                  A->transpose_perm};
   for (void *p : ptrs) if (p) cudaFree(p);
   if (A->stream) cudaStreamDestroy(A->stream);
   for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -597,6 +618,37 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
   default:
     return fail(TBSLA_ERR_INVALID_ARG, "unknown tuning knob %d", knob);
   }
+}
+
+tbsla_status_t tbsla_matrix_set_values(tbsla_matrix_t *A, tbsla_dtype_t type, const void *d_values, void *stream) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(A->format == TBSLA_FMT_CSR, "tbsla_matrix_set_values needs a CSR handle");
+  TB_CHECK(A->values[0], "tbsla_matrix_set_values needs the F64 value store");
+  TB_CHECK(A->stored == 0 || d_values, "values is NULL");
+  TB_CHECK(type == TBSLA_F64 || type == TBSLA_F32, "type must be TBSLA_F64 or TBSLA_F32");
+  TB_CUDA(cudaSetDevice(A->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = A->stored;
+  if (n) {
+    if (type == TBSLA_F64)
+      TB_CUDA(cudaMemcpyAsync(A->values[0], d_values, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+    else
+      f32_to_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(static_cast<const float *>(d_values),
+                                                         static_cast<double *>(A->values[0]), n);
+  }
+  TB_TRY(rederive_stores(A, s));
+  TB_TRY(transpose_refresh(A, s));
+  TB_CUDA(cudaStreamSynchronize(s));
+  // PageRank state derived from the values: rebuilt on next use
+  if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
+  A->pr_work = nullptr;
+  if (A->pr_relabel) free_handle(A->pr_relabel);
+  A->pr_relabel = nullptr;
+  if (A->pr_newid) cudaFree(A->pr_newid);
+  A->pr_newid = nullptr;
+  A->pr_newid_host.clear();
+  A->pr_relabel_state = 0;
+  return TBSLA_OK;
 }
 
 tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A) {

@@ -45,7 +45,7 @@ struct PrCtl {
   int inner_iter, inner_done, inner_max, pad;
 };
 
-enum { kSweepRef = 0, kSweepDang = 1, kSweepInner = 2 };
+enum { kSweepRef = 0, kSweepDang = 1, kSweepInner = 2, kSweepTele = 3 };
 
 // Block reduction of three per-thread values into partials[blk*3 + k]
 // (sums, or a maximum for k = 0 when take_max): values go to shared memory,
@@ -88,6 +88,7 @@ template <typename YT, typename AccT> struct PrEpi {
   const YT *rvec;               // inner sweeps: + r
   const unsigned char *dmask;   // dangling columns (sums b)
   const unsigned char *tmask;   // reference mode with nodes: teleport only there
+  const double *tvec;           // teleport mode: the teleport vector
   const double *add;            // device scalar
   const double *betap;          // device scalar (the damping of this run)
   const int *done;              // device flag: sweep inactive when set
@@ -104,7 +105,8 @@ template <typename YT, typename AccT> struct PrEpi {
       val = f;
       st.a += fabs(val - (double)xold[row]);
     } else {
-      const double t = (mode == kSweepRef && tmask) ? (tmask[row] ? *add : 0.0) : *add;
+      const double t = mode == kSweepTele ? *add * tvec[row]
+                       : (mode == kSweepRef && tmask) ? (tmask[row] ? *add : 0.0) : *add;
       val = __fma_rn(beta, (double)v, t);
       if (mode == kSweepRef) st.a = fmax(st.a, val);
       else st.a += fabs(val - (double)xold[row]);
@@ -120,6 +122,56 @@ template <typename YT, typename AccT> struct PrEpi {
   }
   __device__ __forceinline__ void fixup_done(State &st, int blk) const { block_done(st, blk); }
 };
+
+// Adjoint sweep epilogue, run on the transposed copy (row j = column j of
+// A): lambda'[j] = beta * (A^T lambda)[j] + w[j] + (dangling[j] ? c1 : 0)
+// with c1 = beta * (v . lambda); partials |lambda' - lambda| and v . lambda'.
+struct AdjEpi {
+  using Acc = double;
+  static constexpr bool kReduces = true;
+  struct State {
+    double a = 0, b = 0, c = 0;
+  };
+  double *y;
+  const double *yold;
+  const double *w;
+  const unsigned char *dmask;
+  const double *v;      // teleport vector, NULL: uniform 1/n
+  const double *c1;     // device scalar
+  const double *betap;
+  const int *done;
+  double *partials;
+  double inv_n;
+  int n, part_base;
+  __device__ __forceinline__ bool active() const { return *(volatile const int *)done == 0; }
+  __host__ __device__ void set_part_base(int k) { part_base = k; }
+  __device__ __forceinline__ void emit(int row, double acc, State &st) const {
+    if (row < 0 || row >= n) return;
+    const double val = __fma_rn(*betap, acc, w[row] + (dmask[row] ? *c1 : 0.0));
+    st.a += fabs(val - yold[row]);
+    st.b += (v ? v[row] : inv_n) * val;
+    __stcs(y + row, val);
+  }
+  __device__ __forceinline__ void block_done(State &st, int blk) const {
+    block_reduce3(st.a, st.b, st.c, false, partials, part_base + blk);
+  }
+  __device__ __forceinline__ void fixup_done(State &st, int blk) const { block_done(st, blk); }
+};
+
+// partial (0, v . x (or sum(x)/n), 0)
+__global__ void __launch_bounds__(256) pr_dot_kernel(const double *__restrict__ x, const double *__restrict__ v,
+                                                     int n, double inv_n, double *partials) {
+  double d = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    d += (v ? v[i] : inv_n) * x[i];
+  block_reduce3(0.0, d, 0.0, false, partials, blockIdx.x);
+}
+
+// out = (*s) * x
+__global__ void pr_scale_to_kernel(const double *__restrict__ x, int n, const double *s, double *__restrict__ out) {
+  const double f = *s;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = f * x[i];
+}
 
 // y = beta*(A x) + add (+r) over rows [0, n) from a plain product in `prod`:
 // the path for formats whose kernels do not visit every row
@@ -151,7 +203,9 @@ __global__ void __launch_bounds__(256) pr_normalize_kernel(double *__restrict__ 
 __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restrict__ partials, int nparts,
                                                           PrCtl *ctl, int stage) {
   const bool inner = stage == 3;
-  if (stage <= 3 && (inner ? *(volatile int *)&ctl->inner_done : *(volatile int *)&ctl->done)) return;
+  if ((stage <= 3 || stage == 8 || stage == 10) &&
+      (inner ? *(volatile int *)&ctl->inner_done : *(volatile int *)&ctl->done))
+    return;
   __shared__ double sh[3][256];
   const int t = threadIdx.x;
   const bool take_max = stage == 0;
@@ -213,6 +267,29 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
     break;
   case 7:  // plain sum of a vector (final normalisation)
     ctl->s = c;
+    break;
+  case 8:  // teleport sweep: resid = a, dangling mass = b, sum = c
+    ctl->resid = a;
+    ctl->d = b;
+    ctl->s = c;
+    ctl->iter += 1;
+    ctl->add = ctl->beta * b + (1.0 - ctl->beta);
+    ctl->converged = a < ctl->tol;
+    ctl->done = ctl->converged || ctl->iter >= ctl->max_iter;
+    break;
+  case 9:  // initial teleport-mode vector: dangling mass b
+    ctl->add = ctl->beta * b + (1.0 - ctl->beta);
+    ctl->s = c;
+    break;
+  case 10:  // adjoint sweep: resid = a, b = v . lambda
+    ctl->resid = a;
+    ctl->iter += 1;
+    ctl->add = ctl->beta * b;
+    ctl->converged = a < ctl->tol;
+    ctl->done = ctl->converged || ctl->iter >= ctl->max_iter;
+    break;
+  case 11:  // initial adjoint vector: b = v . lambda0
+    ctl->add = ctl->beta * b;
     break;
   }
 }
@@ -282,6 +359,10 @@ struct PrWork {
   float *prod32 = nullptr;
   float *r = nullptr;
   unsigned char *dmask = nullptr, *tmask = nullptr;
+  double *tvec = nullptr;             // teleport mode: copy of the teleport vector
+  double *lam[2] = {nullptr, nullptr};  // adjoint iterates
+  double *adj_partials = nullptr;
+  int adj_nparts = 0;
   double *partials = nullptr;
   int nparts = 0;
   PrCtl *ctl = nullptr;
@@ -293,7 +374,8 @@ struct PrWork {
   std::vector<G> graphs;
   ~PrWork() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
-    void *ps[] = {x[0], x[1], prod, e[0], e[1], prod32, r, dmask, tmask, partials, ctl};
+    void *ps[] = {x[0], x[1], prod, e[0], e[1], prod32, r, dmask, tmask, tvec, lam[0], lam[1], adj_partials,
+                  partials, ctl};
     for (void *p : ps) if (p) cudaFree(p);
     if (ctl_host) cudaFreeHost(ctl_host);
     if (stream) cudaStreamDestroy(stream);
@@ -396,8 +478,9 @@ static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const 
   epi.y = x_out;
   epi.xold = x_in;
   epi.rvec = nullptr;
-  epi.dmask = mode == kSweepDang ? W->dmask : nullptr;
+  epi.dmask = mode == kSweepDang || mode == kSweepTele ? W->dmask : nullptr;
   epi.tmask = with_tmask ? W->tmask : nullptr;
+  epi.tvec = mode == kSweepTele ? W->tvec : nullptr;
   epi.add = &W->ctl->add;
   epi.betap = &W->ctl->beta;
   epi.done = &W->ctl->done;
@@ -419,7 +502,7 @@ static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const 
     pr_normalize_kernel<<<kAffineBlocks, 256, 0, s>>>(x_out, x_in, W->n, W->ctl, W->partials);
     pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 1);
   } else {
-    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, 2);
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, mode == kSweepTele ? 8 : 2);
   }
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
@@ -520,12 +603,16 @@ tbsla_status_t pr_relabel_gather(const tbsla_matrix *A, const double *x, double 
 using namespace tbsla;
 
 static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const int *nodes,
-                                    int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user) {
+                                    int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user,
+                                    const double *d_teleport = nullptr) {
   TB_CHECK(A && p, "NULL argument");
   TB_CHECK(A->n_row == A->n_col, "PageRank needs a square matrix (%d x %d)", A->n_row, A->n_col);
   TB_CHECK(A->n_col > 0, "empty matrix");
   TB_CHECK(p->max_iter >= 0, "max_iter < 0");
-  TB_CHECK(p->mode == TBSLA_PR_REFERENCE || p->mode == TBSLA_PR_DANGLING, "unknown PageRank mode %d", p->mode);
+  TB_CHECK(p->mode == TBSLA_PR_REFERENCE || p->mode == TBSLA_PR_DANGLING || p->mode == TBSLA_PR_TELEPORT,
+           "unknown PageRank mode %d", p->mode);
+  TB_CHECK(p->mode != TBSLA_PR_TELEPORT || (d_teleport && p->precision == TBSLA_F64),
+           "the teleport mode needs a teleport vector and FP64");
   TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32 || p->precision == TBSLA_BF16, "bad precision");
   TB_CHECK(p->precision == TBSLA_F64 || p->mode == TBSLA_PR_DANGLING, "reduced precision needs TBSLA_PR_DANGLING");
   TB_CHECK(A->values[0], "PageRank needs the F64 value store");
@@ -573,7 +660,13 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   c.done = p->max_iter == 0;
   TB_TRY(write_ctl(W));
   const int g = kAffineBlocks;
-  if (p->mode == TBSLA_PR_REFERENCE) {
+  if (p->mode == TBSLA_PR_TELEPORT) {
+    if (!W->tvec) TB_TRY(pr_alloc((void **)&W->tvec, (size_t)n * 8));
+    TB_CUDA(cudaMemcpyAsync(W->tvec, d_teleport, (size_t)n * 8, cudaMemcpyDeviceToDevice, W->stream));
+    TB_CUDA(cudaMemcpyAsync(W->x[0], d_teleport, (size_t)n * 8, cudaMemcpyDeviceToDevice, W->stream));
+    pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(W->x[0], n, W->dmask, W->partials);
+    pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 9);
+  } else if (p->mode == TBSLA_PR_REFERENCE) {
     pr_fill_kernel<<<g, 256, 0, W->stream>>>(W->x[0], n, with_tmask ? 0.25 : 1.0);
     pr_mass_kernel<double><<<g, 256, 0, W->stream>>>(W->x[0], n, nullptr, W->partials);
     pr_finalize_kernel<<<1, 256, 0, W->stream>>>(W->partials, g, W->ctl, 6);
@@ -586,7 +679,8 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
 
   int f64_sweeps = 0, inner_total = 0;
   if (p->precision == TBSLA_F64) {
-    if (!c.done) TB_TRY(run_f64(A, W, p->mode == TBSLA_PR_REFERENCE ? kSweepRef : kSweepDang, with_tmask, K));
+    const int sweep = p->mode == TBSLA_PR_REFERENCE ? kSweepRef : p->mode == TBSLA_PR_TELEPORT ? kSweepTele : kSweepDang;
+    if (!c.done) TB_TRY(run_f64(A, W, sweep, with_tmask, K));
     else TB_TRY(read_ctl(W));
     f64_sweeps = c.iter;
   } else {
@@ -648,17 +742,113 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   return TBSLA_OK;
 }
 
+namespace tbsla {
+tbsla_status_t ensure_transpose(tbsla_matrix *A, tbsla_matrix **T);
+tbsla_status_t grad_values_f64(const tbsla_matrix *A, const double *a, const double *b, double scale, double *out,
+                               cudaStream_t s);
+}  // namespace tbsla
+
+// The adjoint of the TBSLA_PR_TELEPORT fixed point (see tbsla_gb300.h).
+static tbsla_status_t adjoint_impl(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const double *d_v,
+                                   const double *d_x, const double *d_w, double *d_gvals, double *d_gv,
+                                   tbsla_pagerank_result_t *res, cudaStream_t user) {
+  TB_CHECK(A && p && d_x && d_w, "NULL argument");
+  TB_CHECK(A->format == TBSLA_FMT_CSR && A->csr_variant == 0, "the adjoint needs a CSR handle (default variant)");
+  TB_CHECK(A->n_row == A->n_col && A->n_col > 0, "the adjoint needs a square matrix");
+  TB_CHECK(A->values[0], "the adjoint needs the F64 value store");
+  TB_CHECK(p->max_iter >= 0, "max_iter < 0");
+  TB_CUDA(cudaSetDevice(A->device));
+  PrWork *W = nullptr;
+  TB_TRY(pr_setup(A, &W));
+  tbsla_matrix *T = nullptr;
+  TB_TRY(ensure_transpose(A, &T));
+  TB_CHECK(fused_ok(T), "the transposed copy does not take the fused sweep");
+  const int n = W->n;
+  if (!W->lam[0]) {
+    TB_TRY(pr_alloc((void **)&W->lam[0], (size_t)n * 8));
+    TB_TRY(pr_alloc((void **)&W->lam[1], (size_t)n * 8));
+  }
+  const int nparts = std::max(sweep_parts(T, true), kAffineBlocks);
+  if (W->adj_nparts < nparts) {
+    if (W->adj_partials) cudaFree(W->adj_partials);
+    W->adj_partials = nullptr;
+    W->adj_nparts = 0;
+    TB_TRY(pr_alloc((void **)&W->adj_partials, (size_t)nparts * 3 * 8));
+    W->adj_nparts = nparts;
+  }
+  if (user) {
+    cudaEvent_t ev;
+    TB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaEventRecord(ev, user);
+    cudaStreamWaitEvent(W->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  cudaStream_t s = W->stream;
+  PrCtl &c = *W->ctl_host;
+  std::memset(&c, 0, sizeof c);
+  c.beta = p->beta;
+  c.tol = p->tol;
+  c.inv_n = 1.0 / n;
+  c.max_iter = p->max_iter;
+  c.done = p->max_iter == 0;
+  TB_TRY(write_ctl(W));
+  const int g = kAffineBlocks;
+  TB_CUDA(cudaMemcpyAsync(W->lam[0], d_w, (size_t)n * 8, cudaMemcpyDeviceToDevice, s));
+  pr_dot_kernel<<<g, 256, 0, s>>>(W->lam[0], d_v, n, 1.0 / n, W->adj_partials);
+  pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, g, W->ctl, 11);
+  TB_CUDA(cudaGetLastError());
+  const int K = p->check_every > 0 ? p->check_every : 8;
+  int launched = 0;
+  while (!c.done) {
+    for (int k = 0; k < K; ++k, ++launched) {
+      AdjEpi epi{};
+      epi.y = W->lam[(launched + 1) & 1];
+      epi.yold = W->lam[launched & 1];
+      epi.w = d_w;
+      epi.dmask = W->dmask;
+      epi.v = d_v;
+      epi.c1 = &W->ctl->add;
+      epi.betap = &W->ctl->beta;
+      epi.done = &W->ctl->done;
+      epi.partials = W->adj_partials;
+      epi.inv_n = 1.0 / n;
+      epi.n = n;
+      TB_TRY(launch_product<double, double>(T, static_cast<const double *>(T->values[0]), epi.yold, epi, s));
+      pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, sweep_parts(T, true), W->ctl, 10);
+    }
+    TB_CUDA(cudaGetLastError());
+    TB_TRY(read_ctl(W));
+  }
+  const double *lam = W->lam[c.iter & 1];
+  if (d_gv) {
+    // dL/dv = (beta * d . x + 1 - beta) * lambda (stage 9 leaves that factor in ctl->add)
+    pr_mass_kernel<double><<<g, 256, 0, s>>>(d_x, n, W->dmask, W->adj_partials);
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, g, W->ctl, 9);
+    pr_scale_to_kernel<<<g, 256, 0, s>>>(lam, n, &W->ctl->add, d_gv);
+    TB_CUDA(cudaGetLastError());
+  }
+  if (d_gvals) TB_TRY(grad_values_f64(A, lam, d_x, p->beta, d_gvals, s));
+  TB_CUDA(cudaStreamSynchronize(s));
+  if (res) {
+    res->iterations = c.iter;
+    res->iterations_f64 = c.iter;
+    res->residual = c.resid;
+    res->converged = c.converged;
+  }
+  return TBSLA_OK;
+}
+
 // PageRank of A, on its relabelled copy when there is one (pr_relabel.cu);
 // *result points to the vector in A's labels (d_out, or a buffer of A's)
 static tbsla_status_t pagerank_entry(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const int *nodes,
                                      int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user,
-                                     const double **result) {
+                                     const double **result, const double *d_teleport = nullptr) {
   TB_CHECK(A && p, "NULL argument");
   TB_CUDA(cudaSetDevice(A->device));
   tbsla_matrix *B = nullptr;
-  TB_TRY(pr_relabelled(A, &B));
+  if (!d_teleport) TB_TRY(pr_relabelled(A, &B));
   if (!B) {
-    TB_TRY(pagerank_impl(A, p, nodes, n_nodes, d_out, res, user));
+    TB_TRY(pagerank_impl(A, p, nodes, n_nodes, d_out, res, user, d_teleport));
     if (result) *result = d_out ? d_out : pr_result(static_cast<PrWork *>(A->pr_work));
     return TBSLA_OK;
   }
@@ -688,6 +878,25 @@ tbsla_status_t tbsla_pagerank(const tbsla_matrix_t *A, const tbsla_pagerank_para
                               tbsla_pagerank_result_t *result, void *stream) {
   return pagerank_entry(const_cast<tbsla_matrix *>(A), p, nullptr, 0, d_out, result, (cudaStream_t)stream,
                         nullptr);
+}
+
+tbsla_status_t tbsla_pagerank_teleport(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                       const double *d_v, double *d_out, tbsla_pagerank_result_t *result,
+                                       void *stream) {
+  TB_CHECK(p && d_v, "NULL argument");
+  tbsla_pagerank_params_t q = *p;
+  q.mode = TBSLA_PR_TELEPORT;
+  q.precision = TBSLA_F64;
+  return pagerank_entry(const_cast<tbsla_matrix *>(A), &q, nullptr, 0, d_out, result, (cudaStream_t)stream,
+                        nullptr, d_v);
+}
+
+tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                      const double *d_v, const double *d_x, const double *d_w,
+                                      double *d_grad_values, double *d_grad_v,
+                                      tbsla_pagerank_result_t *result, void *stream) {
+  return adjoint_impl(const_cast<tbsla_matrix *>(A), p, d_v, d_x, d_w, d_grad_values, d_grad_v, result,
+                      (cudaStream_t)stream);
 }
 
 tbsla_status_t tbsla_pagerank_host(tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, double *out,
