@@ -208,6 +208,30 @@ tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx,
 tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t nnz, const int *d_row, const int *d_col,
                                       const double *d_values, const double *d_x, double *d_y, void *stream);
 
+/* -------------------------------------------------------------- batches */
+/* Many CSR handles multiplied together: y_m = A_m x_m for every member in
+ * ONE kernel launch (a persistent grid walking row items of every member
+ * with a fixed stride, so sums are deterministic).  No reference
+ * counterpart (the reference multiplies one matrix per call). */
+typedef struct tbsla_batch tbsla_batch_t;
+/* members: count CSR handles on one device, kept alive by the caller */
+tbsla_status_t tbsla_batch_create(int count, const tbsla_matrix_t *const *members, tbsla_batch_t **out);
+/* Binds device vectors (host arrays of count device pointers; FP64 for
+ * TBSLA_F64, FP32 for the F32 / BF16 stores) and the value store to use. */
+tbsla_status_t tbsla_batch_bind(tbsla_batch_t *B, tbsla_dtype_t store, const void *const *d_x, void *const *d_y);
+/* d_mask: count ints on the device, members with 0 are skipped (their y is
+ * left as it is); NULL: every member.  For iterative callers that stop
+ * members independently. */
+tbsla_status_t tbsla_batch_set_mask(tbsla_batch_t *B, const int *d_mask);
+/* persistent grid of 152 x blocks_per_sm blocks (default 6) */
+tbsla_status_t tbsla_batch_tune(tbsla_batch_t *B, int blocks_per_sm);
+/* Enqueues the one launch on `stream`: no allocation, no synchronisation. */
+tbsla_status_t tbsla_batch_spmv(tbsla_batch_t *B, void *stream);
+/* The same launch replayed from a CUDA graph built on the first call (it
+ * reads the member table, so later tbsla_batch_bind calls apply to it). */
+tbsla_status_t tbsla_batch_spmv_graph(tbsla_batch_t *B, void *stream);
+tbsla_status_t tbsla_batch_destroy(tbsla_batch_t *B);
+
 /* ----------------------------------------------------------- PageRank */
 typedef enum {
   /* Matrix::page_rank (Matrix.cpp:13-61): b0 = 1; b = beta*A b + (1-beta)/n *
@@ -275,6 +299,21 @@ tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pager
                                       const double *d_v, const double *d_x, const double *d_w,
                                       double *d_grad_values, double *d_grad_v,
                                       tbsla_pagerank_result_t *result, void *stream);
+
+/* k personalized PageRank vectors of one square CSR graph solved together
+ * (TBSLA_PR_TELEPORT form): vector c teleports uniformly to its seed set
+ * nodes[offsets[c] .. offsets[c+1]) (repeated seeds count once), and stops on
+ * its own when its L1 change is below p->tol or after p->max_iter sweeps;
+ * stopped vectors are frozen while the others continue.  The iterates are
+ * multiplied in tiles of `tile` vectors (8, 16 or 32; 0 picks one) as one
+ * multi-vector product per tile.  p->precision: TBSLA_F64, or TBSLA_F32
+ * (F32 value store and FP32 iterates).  d_out: n*k doubles, vector c at
+ * d_out + c*n; iterations / residuals: k host entries each, or NULL.
+ * Allocates its work buffers (2 n k values of the precision) per call.  No
+ * reference counterpart. */
+tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                 const int *nodes, const int *offsets, int tile, double *d_out, int *iterations,
+                                 double *residuals, void *stream);
 
 /* Matrix::personalized_page_rank (Matrix.cpp:63-114): as TBSLA_PR_REFERENCE
  * with b0 = 0.25 and the teleport term (1-beta)*sum(b_prev)/n_nodes added only

@@ -113,6 +113,14 @@ def lib() -> C.CDLL:
         "tbsla_pagerank_teleport": ([P, C.POINTER(PageRankParams), _vp, _vp, C.POINTER(PageRankResult), _vp], st),
         "tbsla_pagerank_adjoint": ([P, C.POINTER(PageRankParams), _vp, _vp, _vp, _vp, _vp,
                                     C.POINTER(PageRankResult), _vp], st),
+        "tbsla_batch_create": ([C.c_int, C.POINTER(_vp), C.POINTER(_vp)], st),
+        "tbsla_batch_bind": ([_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)], st),
+        "tbsla_batch_set_mask": ([_vp, _vp], st),
+        "tbsla_batch_tune": ([_vp, C.c_int], st),
+        "tbsla_batch_spmv": ([_vp, _vp], st),
+        "tbsla_batch_spmv_graph": ([_vp, _vp], st),
+        "tbsla_batch_destroy": ([_vp], st),
+        "tbsla_ppr_batched": ([P, C.POINTER(PageRankParams), C.c_int, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp], st),
     }
     for name, (args, res) in list(sig.items()) + list(optional.items()):
         if not hasattr(L, name):
@@ -377,3 +385,54 @@ class DeviceMatrix:
         h = _vp()
         check(lib().tbsla_rmat_pagerank_matrix(scale, m, a, b, c, seed, stores, C.byref(h)))
         return cls(h)
+
+
+class Batch:
+    """Several CSR DeviceMatrix objects multiplied in one launch (tbsla_batch_*)."""
+
+    def __init__(self, members):
+        self.members = list(members)  # kept alive while the batch exists
+        arr = (_vp * len(self.members))(*[m.h for m in self.members])
+        self.h = _vp()
+        check(lib().tbsla_batch_create(len(self.members), arr, C.byref(self.h)))
+
+    def bind(self, store: int, d_x, d_y):
+        xs = (_vp * len(d_x))(*d_x)
+        ys = (_vp * len(d_y))(*d_y)
+        check(lib().tbsla_batch_bind(self.h, store, xs, ys))
+
+    def set_mask(self, d_mask):
+        check(lib().tbsla_batch_set_mask(self.h, d_mask))
+
+    def tune(self, blocks_per_sm: int):
+        check(lib().tbsla_batch_tune(self.h, blocks_per_sm))
+
+    def spmv(self, stream=None, graph=False):
+        f = lib().tbsla_batch_spmv_graph if graph else lib().tbsla_batch_spmv
+        check(f(self.h, stream))
+
+    def close(self):
+        if self.h:
+            lib().tbsla_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ppr_batched(A, seed_sets, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, precision=F64, tile=0,
+                stream=None, check_every=0):
+    """k personalized PageRank vectors of A solved together; returns (iterations, residuals)."""
+    k = len(seed_sets)
+    offsets = np.zeros(k + 1, np.int32)
+    offsets[1:] = np.cumsum([len(s) for s in seed_sets])
+    nodes = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int32) for s in seed_sets]), np.int32)
+    its = np.zeros(k, np.int32)
+    res = np.zeros(k, np.float64)
+    p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, precision, check_every)
+    check(lib().tbsla_ppr_batched(A.h, C.byref(p), k, _ptr(nodes), _ptr(offsets), tile, d_out, _ptr(its),
+                                  _ptr(res), stream))
+    return its, res

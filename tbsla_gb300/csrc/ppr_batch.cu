@@ -1,0 +1,432 @@
+// ppr_batch.cu -- many personalized PageRank vectors of one graph solved
+// together (TBSLA_PR_TELEPORT form, one teleport set per vector).
+//
+// The k iterates are kept in tiles of KT columns (KT = 8, 16 or 32), each
+// tile row-major: tile t, row i holds X[i*KT + c] for its KT vectors, so the
+// gather of a column index brings all KT values in one contiguous segment.
+// A group of KT lanes sums a row, lane c for vector c: no cross-lane
+// reduction, every lane does useful multiply-adds.  Rows longer than
+// kPprChunk entries are cut into chunks (partials + a fixup kernel) so that
+// hub rows of power-law graphs spread over many groups.
+//
+// Per vector c with seed set P_c (v_c = 1/|P_c| on P_c):
+//   x_c <- beta A x_c + (beta d.x_c + 1 - beta) v_c,
+// stopped on its own when ||x_c - x_c,prev||_1 < tol (or max_iter sweeps);
+// a stopped vector is frozen (its lanes copy the old value), and a tile
+// whose vectors have all stopped skips its kernels.  All sums have a fixed
+// order: results do not depend on scheduling.
+//
+// Large skewed graphs run on the degree-relabelled copy (pr_relabel.cu);
+// seeds are mapped in and the results gathered back to the original labels.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "product.cuh"
+
+namespace tbsla {
+
+tbsla_status_t pr_relabelled(tbsla_matrix *A, tbsla_matrix **B);
+
+namespace {
+
+constexpr int kPprChunk = 512;
+
+struct ColCtl {
+  double add;    // beta * d.x + 1 - beta of the current iterate
+  double resid;  // last L1 change
+  int iter, done;
+};
+struct TileCtl {
+  int done, iter;  // iter: sweeps run on the tile (parity of the buffer holding it)
+  int pad[2];
+};
+
+// Lane-column sums of a block for (resid, dmass) into partials[(part*KT+c)*2]
+template <int KT>
+__device__ __forceinline__ void block_columns(double r, double d, double *partials, int part) {
+  __shared__ double sh[8][32][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  #pragma unroll
+  for (int o = 16; o >= KT; o >>= 1) {
+    r += __shfl_down_sync(0xffffffffu, r, o);
+    d += __shfl_down_sync(0xffffffffu, d, o);
+  }
+  if (lane < KT) {
+    sh[warp][lane][0] = r;
+    sh[warp][lane][1] = d;
+  }
+  __syncthreads();
+  if (threadIdx.x < KT) {
+    double a = 0, b = 0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) {
+      a += sh[w][threadIdx.x][0];
+      b += sh[w][threadIdx.x][1];
+    }
+    partials[((size_t)part * KT + threadIdx.x) * 2 + 0] = a;
+    partials[((size_t)part * KT + threadIdx.x) * 2 + 1] = b;
+  }
+}
+
+// y for one finished row (all KT lanes of the group)
+template <typename T, int KT>
+__device__ __forceinline__ void ppr_emit(int row, int c, T acc, const T *xo, T *xn, const unsigned *seeds,
+                                         const unsigned char *dmask, const ColCtl *col, const double *inv_size,
+                                         double beta, double &r_acc, double &d_acc) {
+  const ColCtl cc = col[c];
+  const T old = xo[(size_t)row * KT + c];
+  T y;
+  if (cc.done) {
+    y = old;
+  } else {
+    const double t = ((seeds[row] >> c) & 1u) ? cc.add * inv_size[c] : 0.0;
+    y = (T)((double)beta * (double)acc + t);
+    r_acc += fabs((double)y - (double)old);
+  }
+  if (dmask[row]) d_acc += (double)y;
+  xn[(size_t)row * KT + c] = y;
+}
+
+// items: (row, begin, end, chunk slot or -1)
+template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_spmm_kernel(const int4 *__restrict__ items, int n_items,
+                                                      const int *__restrict__ colidx, const T *__restrict__ values,
+                                                      const T *__restrict__ xo, T *__restrict__ xn,
+                                                      const unsigned *__restrict__ seeds,
+                                                      const unsigned char *__restrict__ dmask,
+                                                      const ColCtl *__restrict__ col,
+                                                      const double *__restrict__ inv_size, double beta,
+                                                      T *__restrict__ chunk_partials, double *partials,
+                                                      const TileCtl *tile) {
+  if (*(volatile const int *)&tile->done) return;
+  const int c = threadIdx.x & (KT - 1);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
+  double r_acc = 0, d_acc = 0;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; g < n_items; g += ng) {
+    const int4 it = items[g];
+    T acc = 0;
+    int e = it.y;
+    for (; e + 4 <= it.z; e += 4) {
+      const int c0 = __ldg(colidx + e), c1 = __ldg(colidx + e + 1), c2 = __ldg(colidx + e + 2),
+                c3 = __ldg(colidx + e + 3);
+      const T v0 = __ldg(values + e), v1 = __ldg(values + e + 1), v2 = __ldg(values + e + 2),
+              v3 = __ldg(values + e + 3);
+      const T x0 = __ldg(xo + (size_t)c0 * KT + c), x1 = __ldg(xo + (size_t)c1 * KT + c),
+              x2 = __ldg(xo + (size_t)c2 * KT + c), x3 = __ldg(xo + (size_t)c3 * KT + c);
+      acc = fma(v0, x0, acc);
+      acc = fma(v1, x1, acc);
+      acc = fma(v2, x2, acc);
+      acc = fma(v3, x3, acc);
+    }
+    for (; e < it.z; ++e) acc = fma(__ldg(values + e), __ldg(xo + (size_t)__ldg(colidx + e) * KT + c), acc);
+    if (it.w >= 0) chunk_partials[(size_t)it.w * KT + c] = acc;
+    else ppr_emit<T, KT>(it.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, r_acc, d_acc);
+  }
+  block_columns<KT>(r_acc, d_acc, partials, blockIdx.x);
+}
+
+// rows cut into chunks: crow[h] = (row, first slot), crow[n].y = total slots
+template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__ crow, int n_crow,
+                                                       const T *__restrict__ chunk_partials,
+                                                       const T *__restrict__ xo, T *__restrict__ xn,
+                                                       const unsigned *__restrict__ seeds,
+                                                       const unsigned char *__restrict__ dmask,
+                                                       const ColCtl *__restrict__ col,
+                                                       const double *__restrict__ inv_size, double beta,
+                                                       double *partials, int part_base, const TileCtl *tile) {
+  if (*(volatile const int *)&tile->done) return;
+  const int c = threadIdx.x & (KT - 1);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
+  double r_acc = 0, d_acc = 0;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; g < n_crow; g += ng) {
+    const int2 h = crow[g];
+    T acc = 0;
+    for (int s = h.y; s < crow[g + 1].y; ++s) acc += chunk_partials[(size_t)s * KT + c];
+    ppr_emit<T, KT>(h.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, r_acc, d_acc);
+  }
+  block_columns<KT>(r_acc, d_acc, partials, part_base + blockIdx.x);
+}
+
+// per column: sum the parts in order, advance the column, then the tile
+template <int KT>
+__global__ void ppr_finalize_kernel(const double *__restrict__ partials, int nparts, ColCtl *col, TileCtl *tile,
+                                    double beta, double tol, int max_iter, int k_in_tile, int first) {
+  __shared__ int active;
+  if (threadIdx.x == 0) active = 0;
+  __syncthreads();
+  if (*(volatile int *)&tile->done) return;
+  const int c = threadIdx.x;
+  if (c < KT) {
+    double r = 0, d = 0;
+    for (int p = 0; p < nparts; ++p) {
+      r += partials[((size_t)p * KT + c) * 2 + 0];
+      d += partials[((size_t)p * KT + c) * 2 + 1];
+    }
+    ColCtl &cc = col[c];
+    if (first) {
+      cc.add = beta * d + (1.0 - beta);  // initial vector: only the dangling mass is new
+    } else if (!cc.done) {
+      cc.iter += 1;
+      cc.resid = r;
+      cc.add = beta * d + (1.0 - beta);
+      cc.done = r < tol || cc.iter >= max_iter;
+    } else {
+      cc.add = beta * d + (1.0 - beta);
+    }
+    if (c < k_in_tile && !cc.done) atomicOr(&active, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!first) tile->iter += 1;
+    tile->done = active == 0;
+  }
+}
+
+// x0 = v (seeds), dangling mass of x0 per column
+template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_init_kernel(int n, const unsigned *__restrict__ seeds,
+                                                      const unsigned char *__restrict__ dmask,
+                                                      const double *__restrict__ inv_size, T *__restrict__ x,
+                                                      double *partials) {
+  const int c = threadIdx.x & (KT - 1);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
+  double d_acc = 0;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; i < n; i += ng) {
+    const T v = ((seeds[i] >> c) & 1u) ? (T)inv_size[c] : T(0);
+    x[(size_t)i * KT + c] = v;
+    if (dmask[i]) d_acc += (double)v;
+  }
+  block_columns<KT>(0.0, d_acc, partials, blockIdx.x);
+}
+
+// dmask[j] = 1 when column j holds no nonzero value
+template <typename T>
+__global__ void ppr_dangling_kernel(const int *__restrict__ colidx, const T *__restrict__ values, int64_t nnz,
+                                    unsigned char *dmask) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x)
+    if (values[k] != T(0)) dmask[colidx[k]] = 0;
+}
+
+// out[c*n + v] = tile(c)[map(v)][c % KT] as FP64
+template <typename T, int KT>
+__global__ void ppr_gather_kernel(const T *__restrict__ x, int n, const int *__restrict__ newid, int k_in_tile,
+                                  int col0, double *__restrict__ out) {
+  const int64_t total = (int64_t)n * k_in_tile;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(t / n), v = (int)(t % n);
+    const int i = newid ? newid[v] : v;
+    out[(size_t)(col0 + c) * n + v] = (double)x[(size_t)i * KT + c];
+  }
+}
+
+template <typename T, int KT>
+tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std::vector<int> *newid_host,
+                         const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
+                         double *d_out, int *iters_out, double *resid_out, cudaStream_t s) {
+  const int n = M->n_row;
+  const int64_t nnz = M->stored;
+  const T *values = static_cast<const T *>(M->values[std::is_same<T, double>::value ? 0 : 1]);
+  TB_CHECK(values, "the matrix lacks the %s value store", std::is_same<T, double>::value ? "F64" : "F32");
+  const int tiles = (k + KT - 1) / KT;
+  // work items: rows, and chunks of rows longer than kPprChunk
+  std::vector<int> rp((size_t)n + 1);
+  TB_CUDA(cudaMemcpy(rp.data(), M->idx0, ((size_t)n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int4> items;
+  std::vector<int2> crow;
+  int slots = 0;
+  items.reserve((size_t)n);
+  for (int r = 0; r < n; ++r) {
+    const int a = rp[(size_t)r], b = rp[(size_t)r + 1];
+    if (b - a <= kPprChunk) {
+      items.push_back(make_int4(r, a, b, -1));
+      continue;
+    }
+    crow.push_back(make_int2(r, slots));
+    for (int e = a; e < b; e += kPprChunk) items.push_back(make_int4(r, e, std::min(e + kPprChunk, b), slots++));
+  }
+  const int n_crow = (int)crow.size();
+  crow.push_back(make_int2(-1, slots));
+  // seeds: bit c of seeds[t*n + i] = row i is a seed of vector t*KT + c
+  std::vector<unsigned> seeds((size_t)tiles * n, 0u);
+  std::vector<double> inv((size_t)tiles * KT, 0.0);
+  for (int c = 0; c < k; ++c) {
+    const int b = offsets[c], e = offsets[c + 1];
+    TB_CHECK(e > b, "vector %d has an empty seed set", c);
+    std::vector<int> dist;
+    for (int q = b; q < e; ++q) {
+      int v = nodes[q];
+      TB_CHECK(v >= 0 && v < n, "seed %d of vector %d outside [0, %d)", v, c, n);
+      if (newid_host) v = (*newid_host)[(size_t)v];
+      dist.push_back(v);
+    }
+    std::sort(dist.begin(), dist.end());
+    dist.erase(std::unique(dist.begin(), dist.end()), dist.end());
+    for (int v : dist) seeds[(size_t)(c / KT) * n + v] |= 1u << (c % KT);
+    inv[(size_t)c] = 1.0 / (double)dist.size();
+  }
+  const int grid_mm = kStrideBlocks;
+  const int grid_fx = std::max(1, std::min((n_crow * KT + 255) / 256, 152 * 4));
+  const int grid_in = 152 * 4;
+  const int nparts = std::max(grid_mm + grid_fx, grid_in);
+  // device buffers
+  const size_t xbytes = (size_t)n * KT * sizeof(T);
+  T *x[2] = {nullptr, nullptr};
+  T *chunk = nullptr;
+  int4 *d_items = nullptr;
+  int2 *d_crow = nullptr;
+  unsigned *d_seeds = nullptr;
+  unsigned char *dmask = nullptr;
+  double *d_inv = nullptr, *partials = nullptr;
+  ColCtl *d_col = nullptr;
+  TileCtl *d_tile = nullptr;
+  std::vector<void *> owned;
+  tbsla_status_t st = TBSLA_OK;
+  auto alloc = [&](void **ptr, size_t bytes) {
+    if (st != TBSLA_OK) return;
+    if (cudaMalloc(ptr, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+      cudaGetLastError();
+      st = fail(TBSLA_ERR_OOM, "batched PageRank buffers (%zu bytes)", bytes);
+      return;
+    }
+    owned.push_back(*ptr);
+  };
+  alloc((void **)&x[0], (size_t)tiles * xbytes);
+  alloc((void **)&x[1], (size_t)tiles * xbytes);
+  alloc((void **)&chunk, (size_t)std::max(slots, 1) * KT * sizeof(T));
+  alloc((void **)&d_items, items.size() * sizeof(int4));
+  alloc((void **)&d_crow, crow.size() * sizeof(int2));
+  alloc((void **)&d_seeds, seeds.size() * sizeof(unsigned));
+  alloc((void **)&dmask, (size_t)n);
+  alloc((void **)&d_inv, inv.size() * sizeof(double));
+  alloc((void **)&partials, (size_t)tiles * nparts * KT * 2 * sizeof(double));
+  alloc((void **)&d_col, (size_t)tiles * KT * sizeof(ColCtl));
+  alloc((void **)&d_tile, (size_t)tiles * sizeof(TileCtl));
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(s);
+    for (void *q : owned) cudaFree(q);
+  };
+  if (st != TBSLA_OK) { cleanup(); return st; }
+  std::vector<ColCtl> hcol((size_t)tiles * KT);
+  for (int c = 0; c < tiles * KT; ++c) {
+    hcol[(size_t)c] = ColCtl{0.0, 0.0, 0, c >= k ? 1 : 0};  // padding columns start stopped
+  }
+  std::vector<TileCtl> htile((size_t)tiles, TileCtl{0, 0, {0, 0}});
+  if (p->max_iter == 0)
+    for (auto &tc : htile) tc.done = 1;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void *d, const void *h, size_t b) {
+    if (e == cudaSuccess && b) e = cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, s);
+  };
+  up(d_items, items.data(), items.size() * sizeof(int4));
+  up(d_crow, crow.data(), crow.size() * sizeof(int2));
+  up(d_seeds, seeds.data(), seeds.size() * sizeof(unsigned));
+  up(d_inv, inv.data(), inv.size() * sizeof(double));
+  up(d_col, hcol.data(), hcol.size() * sizeof(ColCtl));
+  up(d_tile, htile.data(), htile.size() * sizeof(TileCtl));
+  if (e == cudaSuccess) e = cudaMemsetAsync(dmask, 1, (size_t)n, s);
+  if (e != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank upload: %s", cudaGetErrorString(e)); }
+  ppr_dangling_kernel<T><<<152 * 8, 256, 0, s>>>(M->idx1, values, nnz, dmask);
+  const double beta = p->beta;
+  for (int t = 0; t < tiles; ++t) {
+    double *pt = partials + (size_t)t * nparts * KT * 2;
+    ppr_init_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, d_seeds + (size_t)t * n, dmask, d_inv + (size_t)t * KT,
+                                                   x[0] + (size_t)t * n * KT, pt);
+    ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, grid_in, d_col + (size_t)t * KT, d_tile + t, beta, p->tol,
+                                             p->max_iter, std::min(KT, k - t * KT), 1);
+  }
+  if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank init"); }
+  // sweeps: each round runs K sweeps on every tile (stopped tiles return at once)
+  const int K = p->check_every > 0 ? p->check_every : 8;
+  std::vector<TileCtl> hdone((size_t)tiles);
+  int rounds = 0;
+  while (true) {
+    for (int k2 = 0; k2 < K; ++k2) {
+      const int sweep = rounds * K + k2;
+      for (int t = 0; t < tiles; ++t) {
+        // tile t runs its sweeps in step with the others until it stops, so
+        // the parity of `sweep` is the parity of its own sweep count
+        const T *xo = x[sweep & 1] + (size_t)t * n * KT;
+        T *xn = x[(sweep + 1) & 1] + (size_t)t * n * KT;
+        double *pt = partials + (size_t)t * nparts * KT * 2;
+        const unsigned *sd = d_seeds + (size_t)t * n;
+        const ColCtl *cl = d_col + (size_t)t * KT;
+        const double *iv = d_inv + (size_t)t * KT;
+        ppr_spmm_kernel<T, KT><<<grid_mm, 256, 0, s>>>(d_items, (int)items.size(), M->idx1, values, xo, xn, sd,
+                                                       dmask, cl, iv, beta, chunk, pt, d_tile + t);
+        if (n_crow)
+          ppr_fixup_kernel<T, KT><<<grid_fx, 256, 0, s>>>(d_crow, n_crow, chunk, xo, xn, sd, dmask, cl, iv, beta,
+                                                          pt, grid_mm, d_tile + t);
+        ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm,
+                                                 d_col + (size_t)t * KT, d_tile + t, beta, p->tol, p->max_iter,
+                                                 std::min(KT, k - t * KT), 0);
+      }
+    }
+    ++rounds;
+    if (cudaMemcpyAsync(hdone.data(), d_tile, hdone.size() * sizeof(TileCtl), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cleanup();
+      return fail(TBSLA_ERR_CUDA, "batched PageRank sweeps failed");
+    }
+    bool all = true;
+    for (auto &tc : hdone) all = all && tc.done;
+    if (all) break;
+  }
+  // results: tile t's last iterate is in x[iter_t % 2]
+  for (int t = 0; t < tiles; ++t) {
+    const T *xf = x[hdone[(size_t)t].iter & 1] + (size_t)t * n * KT;
+    ppr_gather_kernel<T, KT><<<152 * 8, 256, 0, s>>>(xf, n, newid_dev, std::min(KT, k - t * KT), t * KT, d_out);
+  }
+  std::vector<ColCtl> fin((size_t)tiles * KT);
+  if (cudaMemcpyAsync(fin.data(), d_col, fin.size() * sizeof(ColCtl), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cleanup();
+    return fail(TBSLA_ERR_CUDA, "batched PageRank results");
+  }
+  for (int c = 0; c < k; ++c) {
+    if (iters_out) iters_out[c] = fin[(size_t)c].iter;
+    if (resid_out) resid_out[c] = fin[(size_t)c].resid;
+  }
+  cleanup();
+  return TBSLA_OK;
+}
+
+template <typename T>
+tbsla_status_t run_kt(int kt, const tbsla_matrix *M, const int *nd, const std::vector<int> *nh,
+                      const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets, double *out,
+                      int *it, double *rs, cudaStream_t s) {
+  switch (kt) {
+  case 8: return run_tiles<T, 8>(M, nd, nh, p, k, nodes, offsets, out, it, rs, s);
+  case 16: return run_tiles<T, 16>(M, nd, nh, p, k, nodes, offsets, out, it, rs, s);
+  default: return run_tiles<T, 32>(M, nd, nh, p, k, nodes, offsets, out, it, rs, s);
+  }
+}
+
+}  // namespace
+}  // namespace tbsla
+
+using namespace tbsla;
+
+extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                            const int *nodes, const int *offsets, int tile, double *d_out,
+                                            int *iterations, double *residuals, void *stream) {
+  TB_CHECK(A && p && nodes && offsets && d_out, "NULL argument");
+  TB_CHECK(k > 0, "k = %d", k);
+  TB_CHECK(A->format == TBSLA_FMT_CSR && A->csr_variant == 0, "batched PageRank needs a CSR handle");
+  TB_CHECK(A->n_row == A->n_col && A->rows == A->n_row && A->f_col == 0, "batched PageRank needs a square graph");
+  TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32, "precision must be TBSLA_F64 or TBSLA_F32");
+  TB_CHECK(tile == 0 || tile == 8 || tile == 16 || tile == 32, "tile %d not 0, 8, 16 or 32", tile);
+  TB_CUDA(cudaSetDevice(A->device));
+  tbsla_matrix *M = const_cast<tbsla_matrix *>(A);
+  tbsla_matrix *B = nullptr;
+  TB_TRY(pr_relabelled(M, &B));
+  const int *nd = B ? M->pr_newid : nullptr;
+  const std::vector<int> *nh = B ? &M->pr_newid_host : nullptr;
+  const tbsla_matrix *R = B ? B : M;
+  const int kt = tile ? tile : (k >= 32 ? 32 : k >= 16 ? 16 : 8);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->precision == TBSLA_F64) return run_kt<double>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+  return run_kt<float>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+}

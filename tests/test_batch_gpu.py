@@ -1,0 +1,102 @@
+"""Batching on the GPU: many matrices in one launch, and many personalized
+PageRank vectors of one graph solved together.
+
+Multi-matrix batch: every member's product equals the one-matrix product of
+the same handle bit for bit (both sum each row in its stored order), masked
+members are left untouched, the graph-replayed launch gives the same
+vectors.  Batched PageRank: each vector against the FP64 CPU restatement of
+the teleport-form PageRank (oracle/tbsla_oracle.c, orc_pagerank_teleport)
+with the vector's seed distribution, L1 <= 1e-12 and the same number of
+sweeps (within one) for FP64; FP32 iterates within 1e-5 of it.
+"""
+import numpy as np
+import pytest
+
+from test_pagerank_gpu import rmat_csr_oracle
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def test_multi_matrix_batch_matches_single_products(gpu):
+    rng = np.random.default_rng(3)
+    dev = torch.device("cuda")
+    members, xs, ys = [], [], []
+    for m in range(12):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(60000))))
+        c = int(rng.integers(8, 33))
+        members.append(gpu.DeviceMatrix.generate("CSR", "cqmat", n, n, c, 0.1, m + 1,
+                                                 stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16))
+    B = gpu.Batch(members)
+    for store, tdt in ((gpu.F64, torch.float64), (gpu.F32, torch.float32), (gpu.BF16, torch.float32)):
+        xs = [torch.rand(A.info().n_col, dtype=tdt, device=dev) for A in members]
+        ys = [torch.full((A.info().n_row,), float("nan"), dtype=tdt, device=dev) for A in members]
+        B.bind(store, [x.data_ptr() for x in xs], [y.data_ptr() for y in ys])
+        B.spmv()
+        torch.cuda.synchronize()
+        vt = gpu.F64 if store == gpu.F64 else gpu.F32
+        for A, x, y in zip(members, xs, ys):
+            ref = torch.empty_like(y)
+            A.spmv_ex(store, vt, x.data_ptr(), vt, ref.data_ptr(), 0, None)
+            torch.cuda.synchronize()
+            assert torch.equal(y, ref)
+        # the graph replay
+        for y in ys:
+            y.fill_(float("nan"))
+        B.spmv(graph=True)
+        B.spmv(graph=True)
+        torch.cuda.synchronize()
+        for A, x, y in zip(members, xs, ys):
+            ref = torch.empty_like(y)
+            A.spmv_ex(store, vt, x.data_ptr(), vt, ref.data_ptr(), 0, None)
+            torch.cuda.synchronize()
+            assert torch.equal(y, ref)
+    # per-member mask: masked members keep their y
+    mask = torch.tensor([m % 3 != 0 for m in range(12)], dtype=torch.int32, device=dev)
+    B.set_mask(mask.data_ptr())
+    for y in ys:
+        y.fill_(-7.0)
+    B.spmv()
+    torch.cuda.synchronize()
+    for m, y in enumerate(ys):
+        assert bool((y == -7.0).all()) == (m % 3 == 0)
+    B.close()
+
+
+def _seed_sets(rng, n, k):
+    sets = []
+    for _ in range(k):
+        size = int(np.exp(rng.uniform(0, np.log(100))))
+        sets.append(rng.integers(0, n, size))
+    sets[0] = np.array([0, 0, 3])  # repeated seed counts once
+    return sets
+
+
+@pytest.mark.parametrize("tile,relabel", [(8, 0), (16, 0), (32, 1)])
+def test_batched_ppr_matches_oracle(gpu, orc, tile, relabel):
+    scale = 12
+    m = 16 << scale
+    A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=5, stores=gpu.STORE_F64 | gpu.STORE_F32)
+    A.tune(gpu.TUNE_PR_RELABEL, relabel)
+    rp, ci, va, dang = rmat_csr_oracle(orc, scale, m, 5)
+    n = rp.size - 1
+    rng = np.random.default_rng(tile)
+    k = 40
+    sets = _seed_sets(rng, n, k)
+    dev = torch.device("cuda")
+    out = torch.empty(k * n, dtype=torch.float64, device=dev)
+    its, res = gpu.ppr_batched(A, sets, out.data_ptr(), tol=1e-13, max_iter=1000, tile=tile)
+    got = out.cpu().numpy().reshape(k, n)
+    for c in (0, 1, 7, 20, 39):
+        v = np.zeros(n)
+        seeds = np.unique(sets[c])
+        v[seeds] = 1.0 / seeds.size
+        xo, ito, _ = orc.pagerank_teleport(rp, ci, va, dang, v, 0.85, 1e-13, 1000)
+        assert np.abs(got[c] - xo).sum() < 1e-12, c
+        assert abs(int(its[c]) - ito) <= 1 and res[c] < 1e-13
+    # FP32 iterates and store
+    out32 = torch.empty(k * n, dtype=torch.float64, device=dev)
+    its32, res32 = gpu.ppr_batched(A, sets, out32.data_ptr(), tol=1e-6, max_iter=1000, tile=tile,
+                                   precision=gpu.F32)
+    got32 = out32.cpu().numpy().reshape(k, n)
+    assert np.max(np.abs(got32 - got).sum(axis=1)) < 1e-5
