@@ -270,6 +270,200 @@ def pagerank_bench(capi, scale=24):
     return res
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def batching_bench(capi, ppr_scale=22):
+    """64 cqmat matrices (n log-uniform 1e3..1e6, c 8..32, q 0.1, FP32) in one
+    launch vs 64 launches; 256 personalized PageRank vectors (|P| log-uniform
+    1..100) on R-MAT 2^22 solved together vs one at a time."""
+    import torch
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(4)
+    out = {}
+    # ---- multi-matrix batch
+    members, algo = [], 0
+    for m in range(64):
+        n = int(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
+        c = int(rng.integers(8, 33))
+        A = capi.DeviceMatrix.generate("CSR", "cqmat", n, n, c, 0.1, m + 1, stores=capi.STORE_F32)
+        members.append(A)
+        i = A.info()
+        algo += i.stored * 8 + (i.rows + 1) * 4 + i.n_col * 4 + i.n_row * 4
+    xs = [torch.rand(A.info().n_col, dtype=torch.float32, device=dev) for A in members]
+    ys = [torch.empty(A.info().n_row, dtype=torch.float32, device=dev) for A in members]
+    B = capi.Batch(members)
+    B.bind(capi.F32, [x.data_ptr() for x in xs], [y.data_ptr() for y in ys])
+    tuned = B.autotune()
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        B.spmv(s.cuda_stream, graph=True)
+    reps = 20
+    e0, e1 = _events()
+    e0.record(s)
+    for _ in range(reps):
+        B.spmv(s.cuda_stream, graph=True)
+    e1.record(s)
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1) / reps
+    e0.record(s)
+    for _ in range(reps):
+        for A, x, y in zip(members, xs, ys):
+            A.spmv_ex(capi.F32, capi.F32, x.data_ptr(), capi.F32, y.data_ptr(), 0, s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    single_ms = e0.elapsed_time(e1) / reps
+    out["multi_matrix"] = {
+        "matrices": 64, "stored": int(sum(A.info().stored for A in members)), "dtype": "f32",
+        "one_launch_ms": round(batch_ms, 4), "one_launch_GB_s": round(algo / batch_ms / 1e6, 1),
+        "64_launches_ms": round(single_ms, 4), "speedup": round(single_ms / batch_ms, 2),
+        "autotuned_blocks_per_sm": tuned.choice}
+    B.close()
+    del members, xs, ys
+    torch.cuda.empty_cache()
+    # ---- 256 personalized PageRank vectors
+    G = capi.DeviceMatrix.rmat_pagerank(ppr_scale, 16 << ppr_scale, seed=1, stores=capi.STORE_F64 | capi.STORE_F32)
+    n = G.info().n_row
+    k = 256
+    sets = [rng.integers(0, n, int(np.exp(rng.uniform(0, np.log(100))))) for _ in range(k)]
+    res = {"graph": f"R-MAT scale {ppr_scale}, 2^{ppr_scale + 4} draws, seed 1", "vectors": k, "tol": 1e-10}
+    ref = torch.empty(k * n, dtype=torch.float64, device=dev)
+    for name, prec, tol in (("fp64", capi.F64, 1e-10), ("fp32", capi.F32, 1e-6)):
+        t = G.autotune_ppr(k, prec)
+        buf = ref if prec == capi.F64 else torch.empty(k * n, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        its, rs = capi.ppr_batched(G, sets, buf.data_ptr(), tol=tol, max_iter=1000, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        entry = {"tile": t.choice, "s": round(dt, 3), "ms_per_vector": round(dt * 1e3 / k, 3),
+                 "sweeps_min_median_max": [int(its.min()), int(np.median(its)), int(its.max())],
+                 "converged": int((rs < tol).sum())}
+        if prec == capi.F32:
+            entry["max_l1_vs_fp64"] = float((buf.view(k, n) - ref.view(k, n)).abs().sum(dim=1).max().item())
+        res[name] = entry
+    # one vector at a time (teleport form, same stopping rule)
+    v = torch.zeros(n, dtype=torch.float64, device=dev)
+    seeds = np.unique(sets[0])
+    v[torch.from_numpy(seeds).to(dev)] = 1.0 / seeds.size
+    x = torch.empty(n, dtype=torch.float64, device=dev)
+    G.pagerank_teleport(v.data_ptr(), x.data_ptr(), 0.85, 1e-10, 1000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = G.pagerank_teleport(v.data_ptr(), x.data_ptr(), 0.85, 1e-10, 1000)
+    torch.cuda.synchronize()
+    one = time.perf_counter() - t0
+    res["one_vector_fp64"] = {"ms": round(one * 1e3, 3), "sweeps": r.iterations,
+                              "l1_vs_batched": float((x - ref.view(k, n)[0]).abs().sum().item())}
+    res["batched_speedup_per_vector_fp64"] = round(one * 1e3 / res["fp64"]["ms_per_vector"], 2)
+    out["ppr_256"] = res
+    G.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def differentiation_bench(capi, scale=22):
+    """Adjoint PageRank gradients on R-MAT 2^22 (w ~ N(0,1), seed 2) with a
+    finite-difference check on 16 edges; backward of y = A x for cqmat 2^24
+    in FP32 (values gradient and transposed product)."""
+    import torch
+    dev = torch.device("cuda")
+    out = {}
+    G = capi.DeviceMatrix.rmat_pagerank(scale, 16 << scale, seed=1)
+    info = G.info()
+    n, nnz = info.n_row, int(info.stored)
+    w = torch.from_numpy(np.random.default_rng(2).standard_normal(n)).to(dev)
+    v = torch.full((n,), 1.0 / n, dtype=torch.float64, device=dev)
+    x = torch.empty(n, dtype=torch.float64, device=dev)
+    gvals = torch.empty(nnz, dtype=torch.float64, device=dev)
+    gv = torch.empty(n, dtype=torch.float64, device=dev)
+    G.pagerank_teleport(v.data_ptr(), x.data_ptr(), 0.85, 1e-15, 2000)
+    G.pagerank_adjoint(v.data_ptr(), x.data_ptr(), w.data_ptr(), gvals.data_ptr(), gv.data_ptr(), 0.85, n * 1e-15,
+                       2000)  # warm: transposed copy, buffers
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rf = G.pagerank_teleport(v.data_ptr(), x.data_ptr(), 0.85, 1e-15, 2000)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ra = G.pagerank_adjoint(v.data_ptr(), x.data_ptr(), w.data_ptr(), gvals.data_ptr(), gv.data_ptr(), 0.85,
+                            n * 1e-15, 2000)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    # fourth-order differences of the GPU forward on 16 random edges
+    _, _, vals = G.csr_download()
+    base = torch.from_numpy(vals).to(dev)
+    rng = np.random.default_rng(7)
+    errs = []
+    xx = torch.empty_like(x)
+
+    def loss(vals_t):
+        G.set_values(capi.F64, vals_t.data_ptr())
+        G.pagerank_teleport(v.data_ptr(), xx.data_ptr(), 0.85, 1e-16, 3000)
+        torch.cuda.synchronize()
+        return float(torch.sum(w * xx).item())
+
+    gcpu = gvals.cpu().numpy()
+    for e in rng.choice(nnz, 16, replace=False):
+        h = 3e-3 * vals[e]
+        f = []
+        for s_ in (1, -1, 2, -2):
+            t = base.clone()
+            t[int(e)] += s_ * h
+            f.append(loss(t))
+        fd = (8 * (f[0] - f[1]) - (f[2] - f[3])) / (12 * h)
+        errs.append(abs(gcpu[e] - fd) / abs(fd))
+    G.set_values(capi.F64, base.data_ptr())
+    out["pagerank_adjoint"] = {
+        "graph": f"R-MAT scale {scale}, 2^{scale + 4} draws, seed 1", "edges": nnz,
+        "forward_ms": round((t1 - t0) * 1e3, 2), "forward_sweeps": rf.iterations,
+        "adjoint_ms": round((t2 - t1) * 1e3, 2), "adjoint_sweeps": ra.iterations,
+        "fd_edges": 16, "fd_rel_err_max": float(max(errs)), "fd_rel_err_median": float(np.median(errs))}
+    G.close()
+    torch.cuda.empty_cache()
+    # backward of y = A x, cqmat 2^24, FP32
+    N = N_HEADLINE
+    A = capi.DeviceMatrix.generate("CSR", "cqmat", N, N, C_HEADLINE, Q_HEADLINE, 0,
+                                   stores=capi.STORE_F64 | capi.STORE_F32)
+    st = int(A.info().stored)
+    gy = torch.rand(N, dtype=torch.float32, device=dev)
+    xv = torch.rand(N, dtype=torch.float32, device=dev)
+    gx = torch.empty(N, dtype=torch.float32, device=dev)
+    gval = torch.empty(st, dtype=torch.float32, device=dev)
+    t0 = time.perf_counter()
+    A.spmv_transpose_ex(capi.F32, capi.F32, gy.data_ptr(), capi.F32, gx.data_ptr())
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
+        A.spmv_transpose_ex(capi.F32, capi.F32, gy.data_ptr(), capi.F32, gx.data_ptr(), s)
+    reps = 10
+    e0, e1 = _events()
+    e0.record()
+    for _ in range(reps):
+        A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
+    e1.record()
+    torch.cuda.synchronize()
+    gv_ms = e0.elapsed_time(e1) / reps
+    e0.record()
+    for _ in range(reps):
+        A.spmv_transpose_ex(capi.F32, capi.F32, gy.data_ptr(), capi.F32, gx.data_ptr(), s)
+    e1.record()
+    torch.cuda.synchronize()
+    tr_ms = e0.elapsed_time(e1) / reps
+    gv_bytes = st * 8 + (N + 1) * 4 + 2 * N * 4   # colidx in, gradient out, dL/dy and x once
+    tr_bytes = st * 8 + (N + 1) * 4 + 2 * N * 4
+    out["spmv_backward_cqmat_2^24_f32"] = {
+        "stored": st, "grad_values_ms": round(gv_ms, 4), "grad_values_GB_s": round(gv_bytes / gv_ms / 1e6, 1),
+        "transpose_product_ms": round(tr_ms, 4), "transpose_product_GB_s": round(tr_bytes / tr_ms / 1e6, 1),
+        "transpose_build_s": round(build_s, 2)}
+    A.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gb300(args, world, rank, local, pg):
     from tbsla_gb300 import build, capi
     build.build()
@@ -368,6 +562,8 @@ def run_gb300(args, world, rank, local, pg):
     if world == 1 and not args.headline_only:
         line["formats"] = format_sweep(capi, peak)
         line["pagerank"] = pagerank_bench(capi)
+        line["batching"] = batching_bench(capi)
+        line["differentiation"] = differentiation_bench(capi)
     print(json.dumps(line), flush=True)
 
 
@@ -381,12 +577,20 @@ def main():
     ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
+    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation"], default=None,
+                    help="only one section of the full report (profiling cases)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
-    if args.pagerank_only:
+    if args.pagerank_only or args.section:
         from tbsla_gb300 import build, capi
         build.build()
-        print(json.dumps({"pagerank": pagerank_bench(capi, args.rmat_scale)}), flush=True)
+        if args.pagerank_only or args.section == "pagerank":
+            print(json.dumps({"pagerank": pagerank_bench(capi, args.rmat_scale)}), flush=True)
+        elif args.section == "batching":
+            print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22)}),
+                  flush=True)
+        elif args.section == "differentiation":
+            print(json.dumps({"differentiation": differentiation_bench(capi)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)

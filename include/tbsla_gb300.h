@@ -232,6 +232,23 @@ tbsla_status_t tbsla_batch_spmv(tbsla_batch_t *B, void *stream);
 tbsla_status_t tbsla_batch_spmv_graph(tbsla_batch_t *B, void *stream);
 tbsla_status_t tbsla_batch_destroy(tbsla_batch_t *B);
 
+/* ------------------------------------------------------------ autotune */
+/* Tuners: each times its candidates with CUDA events on the caller's data
+ * and keeps the fastest in the handle (results never change, only times).
+ * No reference counterpart. */
+typedef struct {
+  int candidates;   /* candidates timed                         */
+  float best_ms;    /* time of the kept one                     */
+  int choice;       /* spmv: kernel variant; batch: blocks per SM; ppr: tile */
+  double value;     /* spmv: x L2-keep fraction; otherwise = choice */
+} tbsla_autotune_result_t;
+/* CSR kernel variant and TBSLA_TUNE_X_L2_KEEP for the `store` product */
+tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_autotune_result_t *res);
+/* persistent grid of a bound batch */
+tbsla_status_t tbsla_autotune_batch(tbsla_batch_t *B, tbsla_autotune_result_t *res);
+/* tile width of tbsla_ppr_batched for k vectors (used when it gets tile 0) */
+tbsla_status_t tbsla_autotune_ppr(tbsla_matrix_t *A, int k, tbsla_dtype_t precision, tbsla_autotune_result_t *res);
+
 /* ----------------------------------------------------------- PageRank */
 typedef enum {
   /* Matrix::page_rank (Matrix.cpp:13-61): b0 = 1; b = beta*A b + (1-beta)/n *

@@ -46,6 +46,10 @@ class PageRankParams(C.Structure):
                 ("precision", C.c_int), ("check_every", C.c_int)]
 
 
+class AutotuneResult(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("best_ms", C.c_float), ("choice", C.c_int), ("value", C.c_double)]
+
+
 class PageRankResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("iterations_f64", C.c_int), ("residual", C.c_double),
                 ("converged", C.c_int)]
@@ -121,6 +125,9 @@ def lib() -> C.CDLL:
         "tbsla_batch_spmv_graph": ([_vp, _vp], st),
         "tbsla_batch_destroy": ([_vp], st),
         "tbsla_ppr_batched": ([P, C.POINTER(PageRankParams), C.c_int, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp], st),
+        "tbsla_autotune_spmv": ([P, C.c_int, C.POINTER(AutotuneResult)], st),
+        "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
+        "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
     }
     for name, (args, res) in list(sig.items()) + list(optional.items()):
         if not hasattr(L, name):
@@ -361,6 +368,16 @@ class DeviceMatrix:
     def tune(self, knob: int, value: float):
         check(lib().tbsla_matrix_tune(self.h, knob, float(value)))
 
+    def autotune_spmv(self, store: int = F64) -> AutotuneResult:
+        r = AutotuneResult()
+        check(lib().tbsla_autotune_spmv(self.h, store, C.byref(r)))
+        return r
+
+    def autotune_ppr(self, k: int, precision: int = F64) -> AutotuneResult:
+        r = AutotuneResult()
+        check(lib().tbsla_autotune_ppr(self.h, k, precision, C.byref(r)))
+        return r
+
     def set_variant(self, variant: int):
         check(lib().tbsla_matrix_set_variant(self.h, variant))
 
@@ -406,6 +423,11 @@ class Batch:
 
     def tune(self, blocks_per_sm: int):
         check(lib().tbsla_batch_tune(self.h, blocks_per_sm))
+
+    def autotune(self) -> "AutotuneResult":
+        r = AutotuneResult()
+        check(lib().tbsla_autotune_batch(self.h, C.byref(r)))
+        return r
 
     def spmv(self, stream=None, graph=False):
         f = lib().tbsla_batch_spmv_graph if graph else lib().tbsla_batch_spmv

@@ -1,0 +1,178 @@
+// autotune.cu -- choices made by measurement on the operands at hand.
+//
+// Each tuner times its candidates with CUDA events on a private stream
+// (after one untimed run of each, so first-touch costs do not count), keeps
+// the fastest, and stores it where the library reads it: the CSR product's
+// kernel variant and x L2-keep fraction (tbsla_matrix_set_variant /
+// TBSLA_TUNE_X_L2_KEEP), the persistent grid of a matrix batch
+// (tbsla_batch_tune), the tile width of batched PageRank (used when
+// tbsla_ppr_batched is called with tile 0).  Results never depend on these
+// choices, only times do.
+#include <vector>
+
+#include "common.cuh"
+
+extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                            const int *nodes, const int *offsets, int tile, double *d_out,
+                                            int *iterations, double *residuals, void *stream);
+
+using namespace tbsla;
+
+namespace {
+
+struct Timer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  Timer() {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  ~Timer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+template <typename F> tbsla_status_t time_ms(cudaStream_t s, int reps, F run, float *ms) {
+  Timer t;
+  TB_TRY(run());  // untimed
+  TB_CUDA(cudaStreamSynchronize(s));
+  TB_CUDA(cudaEventRecord(t.a, s));
+  for (int r = 0; r < reps; ++r) TB_TRY(run());
+  TB_CUDA(cudaEventRecord(t.b, s));
+  TB_CUDA(cudaEventSynchronize(t.b));
+  TB_CUDA(cudaEventElapsedTime(ms, t.a, t.b));
+  *ms /= reps;
+  return TBSLA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_autotune_result_t *res) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(A->values[store == TBSLA_F64 ? 0 : store == TBSLA_F32 ? 1 : 2], "the value store is not present");
+  TB_CUDA(cudaSetDevice(A->device));
+  const tbsla_dtype_t vt = store == TBSLA_F64 ? TBSLA_F64 : TBSLA_F32;
+  const size_t el = vt == TBSLA_F64 ? 8 : 4;
+  void *x = nullptr, *y = nullptr;
+  TB_CUDA(cudaMalloc(&x, std::max<size_t>((size_t)A->n_col, 1) * el));
+  if (cudaMalloc(&y, std::max<size_t>((size_t)A->n_row, 1) * el) != cudaSuccess) {
+    cudaFree(x);
+    return fail(TBSLA_ERR_OOM, "autotune vectors");
+  }
+  cudaMemset(x, 0, std::max<size_t>((size_t)A->n_col, 1) * el);
+  cudaStream_t s;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  const float keeps[] = {0.0f, 0.3f, 0.6f, 1.0f};
+  const int variants = A->format == TBSLA_FMT_CSR ? 2 : 1;
+  float best = 1e30f;
+  int best_v = A->csr_variant;
+  float best_k = A->x_keep;
+  tbsla_status_t st = TBSLA_OK;
+  int tried = 0;
+  for (int v = 0; v < variants && st == TBSLA_OK; ++v)
+    for (float k : keeps) {
+      if (A->format == TBSLA_FMT_CSR) A->csr_variant = v;
+      A->x_keep = k;
+      float ms = 0;
+      st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
+      if (st != TBSLA_OK) break;
+      ++tried;
+      if (ms < best) { best = ms; best_v = v; best_k = k; }
+      if (v == 1) break;  // the row-block kernel does not read x_keep
+    }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  cudaFree(x);
+  cudaFree(y);
+  A->csr_variant = best_v;
+  A->x_keep = best_k;
+  if (res) {
+    res->candidates = tried;
+    res->best_ms = best;
+    res->choice = best_v;
+    res->value = best_k;
+  }
+  return st;
+}
+
+tbsla_status_t tbsla_autotune_batch(tbsla_batch_t *B, tbsla_autotune_result_t *res) {
+  TB_CHECK(B, "batch is NULL");
+  cudaStream_t s;
+  TB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const int cands[] = {2, 4, 6, 8, 12, 16, 24, 32};
+  float best = 1e30f;
+  int best_c = 6, tried = 0;
+  tbsla_status_t st = TBSLA_OK;
+  for (int c : cands) {
+    st = tbsla_batch_tune(B, c);
+    float ms = 0;
+    if (st == TBSLA_OK) st = time_ms(s, 5, [&] { return tbsla_batch_spmv(B, s); }, &ms);
+    if (st != TBSLA_OK) break;
+    ++tried;
+    if (ms < best) { best = ms; best_c = c; }
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (st == TBSLA_OK) st = tbsla_batch_tune(B, best_c);
+  if (res) {
+    res->candidates = tried;
+    res->best_ms = best;
+    res->choice = best_c;
+    res->value = best_c;
+  }
+  return st;
+}
+
+tbsla_status_t tbsla_autotune_ppr(tbsla_matrix_t *A, int k, tbsla_dtype_t precision, tbsla_autotune_result_t *res) {
+  TB_CHECK(A && k > 0, "bad argument");
+  TB_CHECK(precision == TBSLA_F64 || precision == TBSLA_F32, "precision must be TBSLA_F64 or TBSLA_F32");
+  TB_CUDA(cudaSetDevice(A->device));
+  // k single-seed vectors spread over the graph, 3 sweeps each
+  std::vector<int> nodes((size_t)k), offsets((size_t)k + 1);
+  for (int c = 0; c < k; ++c) {
+    nodes[(size_t)c] = (int)(((long long)c * 7919 + 13) % A->n_row);
+    offsets[(size_t)c] = c;
+  }
+  offsets[(size_t)k] = k;
+  double *out = nullptr;
+  TB_CUDA(cudaMalloc(&out, (size_t)k * A->n_row * sizeof(double)));
+  tbsla_pagerank_params_t p{};
+  p.beta = 0.85;
+  p.tol = 0.0;
+  p.max_iter = 3;
+  p.mode = TBSLA_PR_TELEPORT;
+  p.precision = precision;
+  p.check_every = 3;
+  const int tiles[] = {8, 16, 32};
+  float best = 1e30f;
+  int best_t = 32, tried = 0;
+  tbsla_status_t st = TBSLA_OK;
+  Timer t;
+  for (int tile : tiles) {
+    if (tile > 8 && tile > k) break;
+    st = tbsla_ppr_batched(A, &p, k, nodes.data(), offsets.data(), tile, out, nullptr, nullptr, nullptr);
+    if (st != TBSLA_OK) break;
+    cudaEventRecord(t.a, nullptr);
+    st = tbsla_ppr_batched(A, &p, k, nodes.data(), offsets.data(), tile, out, nullptr, nullptr, nullptr);
+    cudaEventRecord(t.b, nullptr);
+    cudaEventSynchronize(t.b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    if (st != TBSLA_OK) break;
+    ++tried;
+    if (ms < best) { best = ms; best_t = tile; }
+  }
+  cudaFree(out);
+  if (st == TBSLA_OK) A->ppr_tile[precision == TBSLA_F64 ? 0 : 1] = best_t;
+  if (res) {
+    res->candidates = tried;
+    res->best_ms = best;
+    res->choice = best_t;
+    res->value = best_t;
+  }
+  return st;
+}
+
+}  // extern "C"

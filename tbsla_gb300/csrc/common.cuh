@@ -129,6 +129,8 @@ struct tbsla_matrix {
   // holds entry transpose_perm[k'] of this matrix
   tbsla_matrix *transpose = nullptr;
   int *transpose_perm = nullptr;
+  // batched PageRank tile width chosen by tbsla_autotune_ppr (F64, F32); 0: none
+  int ppr_tile[2] = {0, 0};
 
   // host-path staging
   cudaStream_t stream = nullptr;

@@ -425,7 +425,8 @@ extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla
   const int *nd = B ? M->pr_newid : nullptr;
   const std::vector<int> *nh = B ? &M->pr_newid_host : nullptr;
   const tbsla_matrix *R = B ? B : M;
-  const int kt = tile ? tile : (k >= 32 ? 32 : k >= 16 ? 16 : 8);
+  const int tuned = M->ppr_tile[p->precision == TBSLA_F64 ? 0 : 1];
+  const int kt = tile ? tile : tuned ? tuned : (k >= 32 ? 32 : k >= 16 ? 16 : 8);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->precision == TBSLA_F64) return run_kt<double>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
   return run_kt<float>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);

@@ -100,3 +100,39 @@ def test_batched_ppr_matches_oracle(gpu, orc, tile, relabel):
                                    precision=gpu.F32)
     got32 = out32.cpu().numpy().reshape(k, n)
     assert np.max(np.abs(got32 - got).sum(axis=1)) < 1e-5
+
+
+def test_autotuners_keep_results(gpu, orc):
+    """The tuners time candidates and keep the fastest; products and
+    PageRank vectors are the same before and after."""
+    dev = torch.device("cuda")
+    A = gpu.DeviceMatrix.rmat_pagerank(12, 16 << 12, seed=2, stores=gpu.STORE_F64 | gpu.STORE_F32)
+    x = np.random.default_rng(0).uniform(-1, 1, 1 << 12)
+    before = A.spmv_host(x)
+    r = A.autotune_spmv(gpu.F64)
+    assert r.candidates >= 2 and r.best_ms > 0 and r.choice in (0, 1) and 0.0 <= r.value <= 1.0
+    after = A.spmv_host(x)
+    assert np.allclose(after, before, rtol=1e-13, atol=1e-15)
+    sets = [[i * 37 % 4096] for i in range(48)]
+    out0 = torch.empty(48 << 12, dtype=torch.float64, device=dev)
+    gpu.ppr_batched(A, sets, out0.data_ptr(), tol=1e-13, max_iter=500, tile=8)
+    t = A.autotune_ppr(48, gpu.F64)
+    assert t.choice in (8, 16, 32) and t.candidates >= 2
+    out1 = torch.empty(48 << 12, dtype=torch.float64, device=dev)
+    gpu.ppr_batched(A, sets, out1.data_ptr(), tol=1e-13, max_iter=500)  # tile 0: the tuned one
+    assert float((out1 - out0).abs().sum()) < 1e-11
+    members = [gpu.DeviceMatrix.generate("CSR", "cqmat", 3000 + 500 * m, 3000 + 500 * m, 10, 0.1, m + 1)
+               for m in range(6)]
+    B = gpu.Batch(members)
+    xs = [torch.rand(M.info().n_col, dtype=torch.float64, device=dev) for M in members]
+    ys = [torch.empty(M.info().n_row, dtype=torch.float64, device=dev) for M in members]
+    B.bind(gpu.F64, [v.data_ptr() for v in xs], [v.data_ptr() for v in ys])
+    B.spmv()
+    torch.cuda.synchronize()
+    ref = [y.clone() for y in ys]
+    b = B.autotune()
+    assert b.choice >= 1 and b.candidates >= 4
+    B.spmv()
+    torch.cuda.synchronize()
+    assert all(torch.equal(y, r0) for y, r0 in zip(ys, ref))
+    B.close()
