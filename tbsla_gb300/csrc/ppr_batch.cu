@@ -414,7 +414,7 @@ extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla
                                             int *iterations, double *residuals, void *stream) {
   TB_CHECK(A && p && nodes && offsets && d_out, "NULL argument");
   TB_CHECK(k > 0, "k = %d", k);
-  TB_CHECK(A->format == TBSLA_FMT_CSR && A->csr_variant == 0, "batched PageRank needs a CSR handle");
+  TB_CHECK(A->format == TBSLA_FMT_CSR, "batched PageRank needs a CSR handle");
   TB_CHECK(A->n_row == A->n_col && A->rows == A->n_row && A->f_col == 0, "batched PageRank needs a square graph");
   TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32, "precision must be TBSLA_F64 or TBSLA_F32");
   TB_CHECK(tile == 0 || tile == 8 || tile == 16 || tile == 32, "tile %d not 0, 8, 16 or 32", tile);

@@ -34,6 +34,41 @@ __global__ void __launch_bounds__(256) grad_short_kernel(const int *__restrict__
   }
 }
 
+// All rows short and consecutive: a warp takes 32 rows [r0, r0 + 32) and
+// strides its lanes over the segment's entries, so index loads and gradient
+// stores are coalesced; a lane finds the row of its entry by a binary search
+// over the 32 row starts held one per lane (shuffles).  The entry loop runs
+// in whole warps (inactive lanes search too, then store nothing), as the
+// full-mask shuffles require.
+template <typename T>
+__global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *__restrict__ rowptr,
+                                                          const int *__restrict__ colidx, int f_col,
+                                                          const T *__restrict__ a, const T *__restrict__ b,
+                                                          T scale, T *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < rows; w += nwarps) {
+    const int r0 = (int)(w * 32);
+    const int mine = min(r0 + lane, rows);
+    const int start = __ldg(rowptr + mine);                    // row start of row r0 + lane
+    const T ar = r0 + lane < rows ? scale * a[r0 + lane] : T(0);
+    const int first = __shfl_sync(0xffffffffu, start, 0);
+    const int end = __ldg(rowptr + min(r0 + 32, rows));
+    for (int e0 = first; e0 < end; e0 += 32) {
+      const int e = e0 + lane;
+      int j = 0;  // largest lane index with start <= e
+      #pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const int cand = j + step;
+        const int v = __shfl_sync(0xffffffffu, start, cand & 31);
+        if (cand < 32 && v <= e) j = cand;
+      }
+      const T arow = __shfl_sync(0xffffffffu, ar, j);
+      if (e < end) out[e] = arow * b[__ldg(colidx + e) - f_col];
+    }
+  }
+}
+
 // the same over the long-row items, L lanes per item
 template <int L, typename T>
 __global__ void __launch_bounds__(256) grad_group_kernel(const int4 *__restrict__ items, int n_items,
@@ -61,6 +96,13 @@ bool csr_direct(const tbsla_matrix *A) { return A && A->format == TBSLA_FMT_CSR 
 template <typename T>
 tbsla_status_t grad_values(const tbsla_matrix *A, const T *a, const T *b, T scale, T *out, cudaStream_t s) {
   if (A->stored == 0 || A->rows == 0) return TBSLA_OK;
+  if (A->short_rows == nullptr && A->n_short == A->rows) {  // every row short, in order
+    const int warps = (A->rows + 31) / 32;
+    grad_segment_kernel<T><<<(int)std::min<int64_t>(((int64_t)warps + 7) / 8, 152 * 64), 256, 0, s>>>(
+        A->rows, A->idx0, A->idx1, A->f_col, a, b, scale, out);
+    TB_CUDA(cudaGetLastError());
+    return TBSLA_OK;
+  }
   if (A->n_short > 0)
     grad_short_kernel<T><<<(int)(((int64_t)A->n_short + 255) / 256), 256, 0, s>>>(
         A->short_rows, A->n_short, A->idx0, A->idx1, A->f_col, a, b, scale, out);

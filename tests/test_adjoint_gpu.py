@@ -77,6 +77,33 @@ def test_transpose_product_and_values_gradient(gpu):
     assert np.allclose(out.cpu().numpy(), S2.T @ gy, rtol=1e-12, atol=1e-12)
 
 
+def test_values_gradient_all_short_rows(gpu):
+    """Every row short (the warp-segment kernel): bit-exact in FP64 and FP32,
+    including empty rows and a row count that is not a multiple of 32."""
+    rng = np.random.default_rng(9)
+    n_row, n_col = 100003, 7000
+    lens = rng.integers(0, 20, n_row)
+    lens[::7] = 0
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    ci = rng.integers(0, n_col, rp[-1]).astype(np.int32)
+    vals = rng.uniform(-1, 1, rp[-1])
+    A = gpu.DeviceMatrix.csr(n_row, n_col, rp, ci, vals, stores=gpu.STORE_F64 | gpu.STORE_F32)
+    rows = np.repeat(np.arange(n_row), lens)
+    dev = torch.device("cuda")
+    gy, x = rng.uniform(-1, 1, n_row), rng.uniform(-1, 1, n_col)
+    tgy, tx = torch.from_numpy(gy).to(dev), torch.from_numpy(x).to(dev)
+    gv = torch.full((vals.size,), float("nan"), dtype=torch.float64, device=dev)
+    A.grad_values(gpu.F64, tgy.data_ptr(), tx.data_ptr(), 1.0, gv.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(gv.cpu().numpy(), gy[rows] * x[ci])
+    gy32, x32 = tgy.float(), tx.float()
+    gv32 = torch.full((vals.size,), float("nan"), dtype=torch.float32, device=dev)
+    A.grad_values(gpu.F32, gy32.data_ptr(), x32.data_ptr(), 0.5, gv32.data_ptr())
+    torch.cuda.synchronize()
+    exp32 = (np.float32(0.5) * gy.astype(np.float32)[rows]) * x.astype(np.float32)[ci]
+    assert np.array_equal(gv32.cpu().numpy(), exp32)
+
+
 def _rmat(gpu, orc, scale, seed):
     m = 16 << scale
     A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=seed)
