@@ -46,7 +46,7 @@ WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_short_kernel launch on the 2^24
 # workload, from the ncu capture summarised in
 # profiles/csr_short_kernel_cqmat_2p24.md
-NCU_TRAFFIC_BYTES = None
+NCU_TRAFFIC_BYTES = 5_520_714_287
 
 
 def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):
