@@ -5,9 +5,9 @@
  * The entry points replace the compute behind TBSLA's tbsla::cpp::Matrix*
  * classes (src/cpp/include/tbsla/cpp/Matrix.hpp:9-47) and the C_CPP_* C ABI
  * (src/cpp/interface/c/include/tbsla/cpp/MatrixCSR.h and its siblings).  A
- * matrix handle owns device
- * copies of one matrix in the layout its kernels want (CSR with a merge-path
- * schedule, column-major ELL, row-sorted COO, row-major DENSE).  Plain
+ * matrix handle owns device copies of one matrix in the layout its kernels
+ * want (CSR with rows binned by length, column-major ELL, row-sorted COO,
+ * row-major DENSE).  Plain
  * pointers and sizes only: no C++ or CUDA types cross this boundary; a
  * stream is passed as `void*` (a cudaStream_t, NULL for the legacy stream).
  *
