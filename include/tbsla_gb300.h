@@ -340,6 +340,19 @@ tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_p
                                                 const int *nodes, int n_nodes, double *out,
                                                 int64_t n_out, tbsla_pagerank_result_t *result);
 
+/* ---------------------------------------------------------------- files */
+/* A handle (F64 store) from a file in the reference's binary matrix layout
+ * of `format`, starting at byte `seek`: what Matrix*::read reads
+ * (MatrixCSR.cpp:206-232 and the matching read of each format).  Files the
+ * reference's write produced load as they are. */
+tbsla_status_t tbsla_matrix_read_file(const char *path, int format, int64_t seek, tbsla_matrix_t **out);
+/* A handle (F64 store) of `format` from a Matrix Market file: "matrix
+ * coordinate real general|symmetric" as MatrixCOO::readMM reads it
+ * (MatrixCOO.cpp:230-292, including its echo of the banner and size lines to
+ * stdout), converted as MatrixCSR(COO) / MatrixELL(COO) / MatrixSCOO(COO) /
+ * MatrixDENSE(COO) do.  Other kinds: TBSLA_ERR_UNSUPPORTED. */
+tbsla_status_t tbsla_matrix_read_mm(const char *path, int format, tbsla_matrix_t **out);
+
 /* ---------------------------------------------------------- generators */
 /* Host-side builders of the reference's synthetic matrices, in the
  * reference's own array layout, so that the drop-in classes and the C_CPP_*

@@ -126,6 +126,8 @@ def lib() -> C.CDLL:
         "tbsla_batch_destroy": ([_vp], st),
         "tbsla_ppr_batched": ([P, C.POINTER(PageRankParams), C.c_int, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp], st),
         "tbsla_autotune_spmv": ([P, C.c_int, C.POINTER(AutotuneResult)], st),
+        "tbsla_matrix_read_file": ([C.c_char_p, C.c_int, C.c_int64, C.POINTER(P)], st),
+        "tbsla_matrix_read_mm": ([C.c_char_p, C.c_int, C.POINTER(P)], st),
         "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
         "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
     }
@@ -396,6 +398,18 @@ class DeviceMatrix:
         vv = np.zeros(max(i.stored, 1), np.float64)
         check(lib().tbsla_csr_download(self.h, _ptr(rp), _ptr(ci), _ptr(vv)))
         return rp, ci[: i.stored], vv[: i.stored]
+
+    @classmethod
+    def read_file(cls, path: str, fmt: str, seek: int = 0):
+        h = _vp()
+        check(lib().tbsla_matrix_read_file(path.encode(), FMT[fmt], seek, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_mm(cls, path: str, fmt: str):
+        h = _vp()
+        check(lib().tbsla_matrix_read_mm(path.encode(), FMT[fmt], C.byref(h)))
+        return cls(h)
 
     @classmethod
     def rmat_pagerank(cls, scale, m, a=0.57, b=0.19, c=0.19, seed=1, stores=STORE_F64):
