@@ -46,7 +46,7 @@ def test_matrix_market_into_device(gpu, tmp_path):
     v = rng.uniform(-1, 1, nv)
     gen = tmp_path / "g.mtx"
     gen.write_text("%%MatrixMarket matrix coordinate real general\n% a comment\n"
-                   + f"{nr} {nc} {nv}\n" + "".join(f"{a} {b} {w!r}\n" for a, b, w in zip(r, c, v)))
+                   + f"{nr} {nc} {nv}\n" + "".join(f"{a} {b} {float(w)!r}\n" for a, b, w in zip(r, c, v)))
     dense = np.zeros((nr, nc))
     np.add.at(dense, (r - 1, c - 1), v)
     x = rng.uniform(-1, 1, nc)
@@ -61,7 +61,7 @@ def test_matrix_market_into_device(gpu, tmp_path):
     vs = rng.uniform(-1, 1, rs.size)
     sym = tmp_path / "s.mtx"
     sym.write_text("%%MatrixMarket matrix coordinate real symmetric\n"
-                   + f"{n} {n} {rs.size}\n" + "".join(f"{a} {b} {w!r}\n" for a, b, w in zip(rs, cs, vs)))
+                   + f"{n} {n} {rs.size}\n" + "".join(f"{a} {b} {float(w)!r}\n" for a, b, w in zip(rs, cs, vs)))
     ds = np.zeros((n, n))
     np.add.at(ds, (rs - 1, cs - 1), vs)
     off = rs != cs
