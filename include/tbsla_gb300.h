@@ -133,17 +133,8 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         when the graph is square, has at least 2^20
  *                         vertices, is not banded and its top tenth of
  *                         vertices holds half of the entries.  Results are
- *                         returned in the original labels.
- *   TBSLA_TUNE_CSR_SLABS  1 (default) / 0: use the column slabs of a CSR
- *                         handle for products whose x exceeds 80 MiB.  The
- *                         slabs are built at creation when x in FP64 exceeds
- *                         80 MiB and over 2 % of the entries lie more than
- *                         65536 columns from the diagonal: each holds the
- *                         entries of one column range (x part <= 64 MiB),
- *                         multiplied in turn so that its x part stays in L2;
- *                         they double the matrix's device memory.  Row sums
- *                         are then taken per slab, then added. */
-typedef enum { TBSLA_TUNE_X_L2_KEEP = 0, TBSLA_TUNE_PR_RELABEL = 1, TBSLA_TUNE_CSR_SLABS = 2 } tbsla_tune_knob_t;
+ *                         returned in the original labels. */
+typedef enum { TBSLA_TUNE_X_L2_KEEP = 0, TBSLA_TUNE_PR_RELABEL = 1 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
 

@@ -71,22 +71,17 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   float best_k = A->x_keep;
   tbsla_status_t st = TBSLA_OK;
   int tried = 0;
-  const bool slabs = !A->slabs.empty();
-  bool best_slabs = A->use_slabs;
-  for (int sl = slabs ? 1 : 0; sl >= 0 && st == TBSLA_OK; --sl)
-    for (int v = 0; v < variants && st == TBSLA_OK; ++v)
-      for (float k : keeps) {
-        if (A->format == TBSLA_FMT_CSR) A->csr_variant = v;
-        A->x_keep = k;
-        A->use_slabs = sl == 1;
-        float ms = 0;
-        st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
-        if (st != TBSLA_OK) break;
-        ++tried;
-        if (ms < best) { best = ms; best_v = v; best_k = k; best_slabs = sl == 1; }
-        if (v == 1) break;  // the row-block kernel does not read x_keep
-      }
-  A->use_slabs = best_slabs;
+  for (int v = 0; v < variants && st == TBSLA_OK; ++v)
+    for (float k : keeps) {
+      if (A->format == TBSLA_FMT_CSR) A->csr_variant = v;
+      A->x_keep = k;
+      float ms = 0;
+      st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
+      if (st != TBSLA_OK) break;
+      ++tried;
+      if (ms < best) { best = ms; best_v = v; best_k = k; }
+      if (v == 1) break;  // the row-block kernel does not read x_keep
+    }
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
   cudaFree(x);

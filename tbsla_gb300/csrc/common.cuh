@@ -129,12 +129,6 @@ struct tbsla_matrix {
   // holds entry transpose_perm[k'] of this matrix
   tbsla_matrix *transpose = nullptr;
   int *transpose_perm = nullptr;
-  // CSR column slabs (built at creation when the gathered vector is larger
-  // than L2 and entries reach far from the diagonal): slab k holds the
-  // entries of columns [k*w, (k+1)*w) as a CSR handle of its own, in their
-  // row order, so that each slab's part of x stays in L2 while it streams
-  std::vector<tbsla_matrix *> slabs;
-  bool use_slabs = true;  // TBSLA_TUNE_CSR_SLABS
   // batched PageRank tile width chosen by tbsla_autotune_ppr (F64, F32); 0: none
   int ppr_tile[2] = {0, 0};
 

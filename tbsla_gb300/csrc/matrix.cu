@@ -193,7 +193,6 @@ static void free_handle(tbsla_matrix *A) {
   if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
   if (A->pr_relabel) free_handle(A->pr_relabel);
   if (A->transpose) free_handle(A->transpose);
-  for (tbsla_matrix *S : A->slabs) free_handle(S);
   for (void *p : A->values) if (p) cudaFree(p);
   void *ptrs[] = {A->idx0, A->idx1, A->row_blocks, A->huge_rows, A->huge_partials, A->huge_partials32,
                   A->short_rows, A->warp_items, A->chunk_rows, A->chunk_partials, A->chunk_partials32,
@@ -237,39 +236,12 @@ static int out_shift(const tbsla_matrix *A, int vect_incr) {
   return 0;
 }
 
-// the column slabs serve a plain CSR product whose gathered vector is larger
-// than kSlabXBytes (FP64 x at 2^24; FP32 x of the same matrix fits in L2)
-constexpr int64_t kSlabXBytes = 80ll << 20;
-static bool slabs_apply(const tbsla_matrix *A, size_t x_bytes) {
-  return A->format == TBSLA_FMT_CSR && A->csr_variant == 0 && A->use_slabs && A->slabs.size() > 1 &&
-         A->x_extent * (int64_t)x_bytes > kSlabXBytes;
-}
-
 template <typename V, typename XT, typename YT>
 static tbsla_status_t spmv_typed(const tbsla_matrix *A, const V *vals, const XT *x, YT *y,
                                  int vect_incr, cudaStream_t s) {
   using Acc = typename AccOf<V>::type;
   TB_TRY(zero_unwritten(A, y, sizeof(YT), vect_incr, s));
   if (A->format == TBSLA_FMT_CSR && A->stored == 0) return TBSLA_OK;  // MatrixCSR.cpp:130-131
-  if (slabs_apply(A, sizeof(XT))) {
-    // column slabs: the first stores, the others add; one timed region
-    KernelTimer kt(A, s);
-    const int si = A->values[0] == static_cast<const void *>(vals) ? 0 : A->values[1] == static_cast<const void *>(vals) ? 1 : 2;
-    for (size_t k = 0; k < A->slabs.size(); ++k) {
-      const tbsla_matrix *S = A->slabs[k];
-      const V *sv = static_cast<const V *>(S->values[si]);
-      if (S->stored == 0) continue;
-      if (k == 0) {
-        StoreEpi<YT, Acc> epi{y, A->n_row, 0};
-        TB_TRY(launch_product<V, XT>(S, sv, x, epi, s));
-      } else {
-        AccumEpi<YT, Acc> epi{y, A->n_row};
-        TB_TRY(launch_product<V, XT>(S, sv, x, epi, s));
-      }
-    }
-    kt.stop();
-    return TBSLA_OK;
-  }
   StoreEpi<YT, Acc> epi{y, A->n_row, out_shift(A, vect_incr)};
   return launch_product<V, XT>(A, vals, x, epi, s);
 }
@@ -458,59 +430,6 @@ static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *c
   return TBSLA_OK;
 }
 
-
-// slab handles are created with this counter raised, so they are not split
-static thread_local int g_slab_depth = 0;
-
-// Column slabs of a CSR matrix (see the handle field): built when x in FP64
-// exceeds kSlabXBytes and more than 2 % of the entries lie over 65536
-// columns from the diagonal (a banded matrix gathers locally and gains
-// nothing).  Width: each slab's x at most 64 MiB.
-static tbsla_status_t build_slabs(tbsla_matrix *A, const int *rowptr, const int *colidx, const double *values,
-                                  int stores) {
-  const int rows = A->rows;
-  const int64_t nnz = A->stored;
-  if (A->x_extent * 8 <= kSlabXBytes || nnz == 0) return TBSLA_OK;
-  const int base = rowptr[0];
-  int64_t far = 0;
-  for (int r = 0; r < rows; ++r)
-    for (int k = rowptr[r] - base; k < rowptr[r + 1] - base; ++k) far += std::abs((int64_t)(colidx[k] - A->f_col) - r) > 65536;
-  if (far * 50 <= nnz) return TBSLA_OK;
-  const int64_t per = (64ll << 20) / 8;
-  const int K = (int)((A->x_extent + per - 1) / per);
-  const int64_t w = (A->x_extent + K - 1) / K;
-  std::vector<std::vector<int>> rp((size_t)K, std::vector<int>((size_t)rows + 1, 0));
-  for (int r = 0; r < rows; ++r) {
-    for (int k = rowptr[r] - base; k < rowptr[r + 1] - base; ++k) ++rp[(size_t)((colidx[k] - A->f_col) / w)][(size_t)r + 1];
-  }
-  for (int k = 0; k < K; ++k)
-    for (int r = 0; r < rows; ++r) rp[(size_t)k][(size_t)r + 1] += rp[(size_t)k][(size_t)r];
-  std::vector<std::vector<int>> ci((size_t)K);
-  std::vector<std::vector<double>> va((size_t)K);
-  for (int k = 0; k < K; ++k) {
-    ci[(size_t)k].resize((size_t)std::max(rp[(size_t)k][(size_t)rows], 1));
-    va[(size_t)k].resize((size_t)std::max(rp[(size_t)k][(size_t)rows], 1));
-  }
-  std::vector<int> next((size_t)K);
-  for (int r = 0; r < rows; ++r) {
-    for (int k = 0; k < K; ++k) next[(size_t)k] = rp[(size_t)k][(size_t)r];
-    for (int e = rowptr[r] - base; e < rowptr[r + 1] - base; ++e) {
-      const int k = (int)((colidx[e] - A->f_col) / w);
-      ci[(size_t)k][(size_t)next[(size_t)k]] = colidx[e];
-      va[(size_t)k][(size_t)next[(size_t)k]++] = values[e];
-    }
-  }
-  for (int k = 0; k < K; ++k) {
-    tbsla_matrix_t *S = nullptr;
-    TB_TRY(tbsla_csr_create(A->n_row, A->n_col, A->f_col, rows, rp[(size_t)k].data(), ci[(size_t)k].data(),
-                            va[(size_t)k].data(), stores, &S));
-    S->x_keep = 1.0f;  // a slab's part of x fits in L2: keep all of it
-    A->slabs.push_back(S);
-    A->device_bytes += S->device_bytes;
-  }
-  return TBSLA_OK;
-}
-
 }  // namespace tbsla
 
 using namespace tbsla;
@@ -555,12 +474,7 @@ tbsla_status_t tbsla_csr_create(int n_row, int n_col, int f_col, int rows, const
   if (!A) return fail(TBSLA_ERR_OOM, "host allocation failed");
   A->n_row = n_row; A->n_col = n_col; A->f_col = f_col; A->rows = std::min(rows, n_row);
   static const int zero = 0;
-  tbsla_status_t s = build_csr(A, rows ? rowptr : &zero, colidx, values, stores);
-  if (s == TBSLA_OK && g_slab_depth == 0) {
-    ++g_slab_depth;
-    s = build_slabs(A, rows ? rowptr : &zero, colidx, values, stores);
-    --g_slab_depth;
-  }
+  const tbsla_status_t s = build_csr(A, rows ? rowptr : &zero, colidx, values, stores);
   if (s != TBSLA_OK) { free_handle(A); return s; }
   *out = A;
   return TBSLA_OK;
@@ -697,10 +611,6 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
     A->x_keep = (float)value;
     if (A->pr_relabel) A->pr_relabel->x_keep = (float)value;
     return TBSLA_OK;
-  case TBSLA_TUNE_CSR_SLABS:
-    TB_CHECK(value == 0.0 || value == 1.0, "slab mode %g not 0 or 1", value);
-    A->use_slabs = value != 0.0;
-    return TBSLA_OK;
   case TBSLA_TUNE_PR_RELABEL:
     TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0, "PageRank relabel mode %g not -1, 0 or 1", value);
     A->pr_relabel_mode = (int)value;
@@ -758,13 +668,7 @@ tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *i
   switch (A->format) {
   case TBSLA_FMT_CSR:
     if (A->rows > 0 && A->stored > 0) {
-      if (A->csr_variant == 0 && slabs_apply(A, sizeof(double))) {
-        for (const tbsla_matrix *S : A->slabs) {
-          if (S->stored == 0) continue;
-          k += (S->n_short > 0) + (S->n_chunk_rows > 0);
-          for (int c = 0; c < kGroupClasses; ++c) k += S->item_class_start[c + 1] > S->item_class_start[c];
-        }
-      } else if (A->csr_variant == 0) {
+      if (A->csr_variant == 0) {
         k = (A->n_short > 0) + (A->n_chunk_rows > 0);
         for (int c = 0; c < kGroupClasses; ++c) k += A->item_class_start[c + 1] > A->item_class_start[c];
       }

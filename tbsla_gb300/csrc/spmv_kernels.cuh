@@ -46,22 +46,6 @@ template <typename YT, typename AccT> struct StoreEpi {
   __device__ __forceinline__ void fixup_done(State &, int) const {}
 };
 
-// y += A x  (the column slabs after the first, see matrix.cu)
-template <typename YT, typename AccT> struct AccumEpi {
-  using Acc = AccT;
-  static constexpr bool kReduces = false;
-  struct State {};
-  YT *y;
-  int n_out;
-  __device__ __forceinline__ void emit(int row, Acc v, State &) const {
-    if (row >= 0 && row < n_out) y[row] = (YT)((Acc)y[row] + v);
-  }
-  __device__ __forceinline__ bool active() const { return true; }
-  __host__ __device__ void set_part_base(int) {}
-  __device__ __forceinline__ void block_done(State &, int) const {}
-  __device__ __forceinline__ void fixup_done(State &, int) const {}
-};
-
 // y = A x + x  (the first half of Matrix::a_axpx_, Matrix.cpp:6-11)
 template <typename AccT> struct AddXEpi {
   using Acc = AccT;

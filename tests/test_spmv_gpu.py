@@ -263,19 +263,6 @@ def test_full_size_cqmat_exact_integers(gpu):
     expect[np.diff(g.idx0) == 0] = 0
     assert np.array_equal(y, expect)
     assert y.sum() == gathered.sum()
-    # x of 128 MiB and 10 % random columns: the product runs on column slabs
-    # (row sums per slab, then added); random x against the oracle, with the
-    # slabs and without
-    assert m.info().kernels >= 2
-    from oracle.oracle import Oracle
-    orc = Oracle()
-    o = orc.from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
-    oa = orc.from_layout("CSR", g.geom, g.nnz, np.abs(g.values), g.idx0, g.idx1)
-    xr = np.random.default_rng(3).uniform(-1, 1, n)
-    ref, bound = o.spmv(xr, threads=8), oa.spmv(np.abs(xr), threads=8)
-    for slabs in (1, 0):
-        m.tune(gpu.TUNE_CSR_SLABS, slabs)
-        assert_close(m.spmv_host(xr), ref, bound, 1e-12, f"cqmat 2^24 slabs={slabs}")
 
 
 def test_full_size_cdiag(gpu):
