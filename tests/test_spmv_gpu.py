@@ -263,6 +263,13 @@ def test_full_size_cqmat_exact_integers(gpu):
     expect[np.diff(g.idx0) == 0] = 0
     assert np.array_equal(y, expect)
     assert y.sum() == gathered.sum()
+    # random x against the oracle (x of 128 MiB, 10 % random columns)
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    o = orc.from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
+    oa = orc.from_layout("CSR", g.geom, g.nnz, np.abs(g.values), g.idx0, g.idx1)
+    xr = np.random.default_rng(3).uniform(-1, 1, n)
+    assert_close(m.spmv_host(xr), o.spmv(xr, threads=8), oa.spmv(np.abs(xr), threads=8), 1e-12, "cqmat 2^24")
 
 
 def test_full_size_cdiag(gpu):
