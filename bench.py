@@ -199,18 +199,18 @@ def time_product(capi, A, store, vt, n_row, n_col, reps=10):
     return e0.elapsed_time(e1) / reps
 
 
-def format_sweep(capi, peak):
+def format_sweep(capi, peak, log2n=24):
     """Every format / store of the configuration, device GB/s."""
     import torch
     out = {}
-    n = N_HEADLINE
+    n = 1 << log2n
     cases = [("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
              ("CSR_bf16", "CSR", "cqmat", n, 16, 4, capi.BF16, capi.F32),
              ("ELL_f64", "ELL", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("COO_f64", "COO", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("SCOO_f64", "SCOO", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("DENSE_f64_32768", "DENSE", "cqmat", 32768, 16, 1, capi.F64, capi.F64),
-             ("CSR_f64_cdiag_2^26", "CSR", "cdiag", 1 << 26, 1, 1, capi.F64, capi.F64)]
+             ("CSR_f64_cdiag_2^26", "CSR", "cdiag", 4 * n, 1, 1, capi.F64, capi.F64)]
     for (key, fmt, gen, nn, c, stores, store, vt) in cases:
         A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
         i = A.info()
@@ -577,7 +577,7 @@ def main():
     ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
-    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation"], default=None,
+    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats"], default=None,
                     help="only one section of the full report (profiling cases)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
@@ -589,6 +589,8 @@ def main():
         elif args.section == "batching":
             print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22)}),
                   flush=True)
+        elif args.section == "formats":
+            print(json.dumps({"formats": format_sweep(capi, peaks()[0], args.log2n)}), flush=True)
         elif args.section == "differentiation":
             print(json.dumps({"differentiation": differentiation_bench(capi)}), flush=True)
         return
