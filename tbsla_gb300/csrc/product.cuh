@@ -131,7 +131,7 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
       const int threads = (A->rows + 3) / 4;
       KernelTimer kt(A, s);
       ell_kernel<V, XT, Epi><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                 A->rows_pad, A->max_col, epi);
+                                                                 A->rows_pad, A->max_col, A->x_keep, epi);
       kt.stop();
     }
     break;
