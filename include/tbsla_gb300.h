@@ -340,6 +340,12 @@ tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_p
                                                 const int *nodes, int n_nodes, double *out,
                                                 int64_t n_out, tbsla_pagerank_result_t *result);
 
+/* COO / SCOO handle -> CSR handle, on the device: MatrixCSR(const
+ * MatrixCOO&) (MatrixCSR.cpp:29-74) with entries ordered by (row, column),
+ * equal pairs in input order (the host conversion's arrays, bit for bit).
+ * stores: the value stores of the new handle (the COO handle needs F64). */
+tbsla_status_t tbsla_coo_to_csr(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+
 /* ---------------------------------------------------------------- files */
 /* A handle (F64 store) from a file in the reference's binary matrix layout
  * of `format`, starting at byte `seek`: what Matrix*::read reads

@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
         "tbsla_autotune_spmv": ([P, C.c_int, C.POINTER(AutotuneResult)], st),
         "tbsla_matrix_read_file": ([C.c_char_p, C.c_int, C.c_int64, C.POINTER(P)], st),
         "tbsla_matrix_read_mm": ([C.c_char_p, C.c_int, C.POINTER(P)], st),
+        "tbsla_coo_to_csr": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
         "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
     }
@@ -398,6 +399,12 @@ class DeviceMatrix:
         vv = np.zeros(max(i.stored, 1), np.float64)
         check(lib().tbsla_csr_download(self.h, _ptr(rp), _ptr(ci), _ptr(vv)))
         return rp, ci[: i.stored], vv[: i.stored]
+
+    def to_csr(self, stores=STORE_F64):
+        """CSR handle converted on the device from this COO / SCOO handle."""
+        h = _vp()
+        check(lib().tbsla_coo_to_csr(self.h, stores, C.byref(h)))
+        return DeviceMatrix(h)
 
     @classmethod
     def read_file(cls, path: str, fmt: str, seek: int = 0):

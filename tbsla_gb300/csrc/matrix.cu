@@ -165,6 +165,38 @@ tbsla_status_t rederive_stores(tbsla_matrix *A, cudaStream_t s) {
 
 tbsla_status_t transpose_refresh(tbsla_matrix *A, cudaStream_t s);
 
+// As upload_values, from FP64 values already on the device (d_src, n)
+tbsla_status_t store_values_device(tbsla_matrix *A, const double *d_src, int64_t n, int stores, cudaStream_t s) {
+  if (!(stores & (TBSLA_STORE_F64 | TBSLA_STORE_F32 | TBSLA_STORE_BF16)))
+    return fail(TBSLA_ERR_INVALID_ARG, "no value store requested");
+  double *d64 = nullptr;
+  TB_TRY(alloc_n(A, &d64, n));
+  if (n) TB_CUDA(cudaMemcpyAsync(d64, d_src, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  A->values[0] = d64;
+  A->stores = stores & (TBSLA_STORE_F64 | TBSLA_STORE_F32 | TBSLA_STORE_BF16);
+  if (stores & TBSLA_STORE_F32) {
+    float *d = nullptr;
+    TB_TRY(alloc_n(A, &d, n));
+    A->values[1] = d;
+  }
+  if (stores & TBSLA_STORE_BF16) {
+    __nv_bfloat16 *d = nullptr;
+    TB_TRY(alloc_n(A, &d, n));
+    A->values[2] = d;
+  }
+  TB_TRY(rederive_stores(A, s));
+  TB_CUDA(cudaStreamSynchronize(s));
+  if (!(stores & TBSLA_STORE_F64)) {
+    cudaFree(d64);
+    A->values[0] = nullptr;
+    A->device_bytes -= (int64_t)std::max<int64_t>(n, 1) * 8 + 64;
+  }
+  return TBSLA_OK;
+}
+
+tbsla_matrix *new_matrix(int format);
+void free_matrix(tbsla_matrix *A);
+
 static tbsla_status_t alloc_carries(tbsla_matrix *A) {
   const int nt = std::max(A->num_tiles, 1);
   TB_TRY(alloc_n(A, &A->tile_head_row, nt));
@@ -177,6 +209,8 @@ static tbsla_status_t alloc_carries(tbsla_matrix *A) {
   TB_CUDA(cudaMemset(A->d_err, 0, sizeof(int)));
   return TBSLA_OK;
 }
+
+tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp);
 
 static tbsla_matrix *new_handle(int format) {
   tbsla_matrix *A = new (std::nothrow) tbsla_matrix();
@@ -206,6 +240,10 @@ static void free_handle(tbsla_matrix *A) {
   for (auto &e : A->free_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   delete A;
 }
+
+tbsla_matrix *new_matrix(int format) { return new_handle(format); }
+void free_matrix(tbsla_matrix *A) { free_handle(A); }
+tbsla_status_t alloc_ints(tbsla_matrix *A, int **p, int64_t n) { return alloc_n(A, p, n); }
 
 tbsla_status_t axpy_inplace(double *y, const double *x, int64_t n, cudaStream_t s);
 
@@ -369,6 +407,13 @@ static tbsla_status_t build_csr(tbsla_matrix *A, const int *rowptr, const int *c
   TB_CUDA(cudaMemcpy(A->idx0, rp.data(), ((size_t)rows + 1) * sizeof(int), cudaMemcpyHostToDevice));
   if (nnz) TB_CUDA(cudaMemcpy(A->idx1, colidx, nnz * sizeof(int), cudaMemcpyHostToDevice));
   TB_TRY(upload_values(A, values, nnz, stores));
+  return csr_bins(A, rp);
+}
+
+// The row bins of the direct kernels and the row blocks of variant 1 from the
+// host copy of rowptr (base removed); idx0 / idx1 / values already on the device.
+tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
+  const int rows = A->rows;
   // direct bins: short rows by thread, long rows by warp, huge rows by chunk
   {
     std::vector<int> shorts;
