@@ -13,7 +13,7 @@ def _check(gpu, orc, n_row, n_col, row, col, val):
     C = gpu.DeviceMatrix.coo(n_row, n_col, row, col, val)
     A = C.to_csr()
     rp, ci, va = A.csr_download()
-    o = orc.from_arrays("COO", n_row, n_col, val, row, col).convert("CSR").arrays()
+    o = orc.from_arrays("COO", n_row, n_col, val, row, col).convert("CSR").arrays
     assert np.array_equal(rp, o.idx0)
     assert np.array_equal(ci, o.idx1)
     assert np.array_equal(va, o.values)
