@@ -230,7 +230,34 @@ def format_sweep(capi, peak, log2n=24):
                     "stored": int(i.stored), "gflops": round(2 * i.stored / (ms * 1e-3) / 1e9, 1)}
         A.close()
         torch.cuda.empty_cache()
+    out["DENSE_multi_vector_32768_k64"] = dense_multi(capi, 32768 if log2n >= 24 else 8192, 64)
     return out
+
+
+def dense_multi(capi, n, k):
+    """Y = A X for k vectors (cuBLAS GEMM; tensor cores for the BF16 store)."""
+    import torch
+    A = capi.DeviceMatrix.generate("DENSE", "cqmat", n, n, 16, Q_HEADLINE, 0, stores=capi.STORE_F64 | capi.STORE_BF16)
+    res = {}
+    for name, store, tdt in (("f64", capi.F64, torch.float64), ("bf16", capi.BF16, torch.float32)):
+        X = torch.rand((k, n), dtype=tdt, device="cuda")
+        Y = torch.empty((k, n), dtype=tdt, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        for _ in range(3):
+            A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s)
+        e0, e1 = _events()
+        e0.record()
+        for _ in range(5):
+            A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        vb = 8 if store == capi.F64 else 2
+        res[name] = {"ms": round(ms, 3), "TFLOP_s": round(2.0 * n * n * k / ms / 1e9, 1),
+                     "GB_s": round((n * n * vb + 2 * n * k * (8 if store == capi.F64 else 4)) / ms / 1e6, 1)}
+    A.close()
+    torch.cuda.empty_cache()
+    return res
 
 
 def pagerank_bench(capi, scale=24):

@@ -182,6 +182,15 @@ tbsla_status_t tbsla_csr_grad_values(const tbsla_matrix_t *A, tbsla_dtype_t type
 tbsla_status_t tbsla_matrix_set_values(tbsla_matrix_t *A, tbsla_dtype_t type, const void *d_values,
                                        void *stream);
 
+/* Y = A X for a DENSE handle and k vectors: X column-major ln_col x k (leading
+ * dimension ldx), Y column-major n_row x k (ldy); rows past ln_row give 0.
+ * A plain GEMM, done by cuBLAS: FP64 vectors for the F64 store, FP32 for F32
+ * and BF16 (the BF16 store runs on the tensor cores with X rounded to BF16,
+ * FP32 accumulation).  No reference counterpart (the reference multiplies one
+ * vector). */
+tbsla_status_t tbsla_dense_spmm(const tbsla_matrix_t *A, tbsla_dtype_t store, int k, const void *d_X,
+                                int64_t ldx, void *d_Y, int64_t ldy, void *stream);
+
 /* r = A (A x + x): Matrix::a_axpx_ (Matrix.cpp:6-11), square matrices; the
  * "+ x" is fused into the first product.  d_tmp: n_row doubles of scratch or
  * NULL to use the handle's own. */

@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
         "tbsla_matrix_read_file": ([C.c_char_p, C.c_int, C.c_int64, C.POINTER(P)], st),
         "tbsla_matrix_read_mm": ([C.c_char_p, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_csr": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_dense_spmm": ([P, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp], st),
         "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
         "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
     }
@@ -399,6 +400,9 @@ class DeviceMatrix:
         vv = np.zeros(max(i.stored, 1), np.float64)
         check(lib().tbsla_csr_download(self.h, _ptr(rp), _ptr(ci), _ptr(vv)))
         return rp, ci[: i.stored], vv[: i.stored]
+
+    def dense_spmm(self, store: int, k: int, d_X: int, ldx: int, d_Y: int, ldy: int, stream=None):
+        check(lib().tbsla_dense_spmm(self.h, store, k, d_X, ldx, d_Y, ldy, stream))
 
     def to_csr(self, stores=STORE_F64):
         """CSR handle converted on the device from this COO / SCOO handle."""
