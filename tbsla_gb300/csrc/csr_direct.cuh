@@ -144,10 +144,36 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
   typename Epi::State es{};
   const uint64_t keep = policy_keep(x_keep);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_rows; t += stride) {
-    const int r = rows ? __ldg(rows + t) : (int)t;
-    const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
-    epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if constexpr (!Epi::kReduces) {
+    // one row per thread (uncapped grid)
+    for (; t < n_rows; t += stride) {
+      const int r = rows ? __ldg(rows + t) : (int)t;
+      const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
+      epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
+    }
+  } else {
+    // the next row's bounds are loaded before the current row is summed, so
+    // their latency overlaps the sum (capped grids give a thread many rows)
+    int r = 0, a = 0, b = 0;
+    if (t < n_rows) {
+      r = rows ? __ldg(rows + t) : (int)t;
+      a = __ldg(rowptr + r);
+      b = __ldg(rowptr + r + 1);
+    }
+    for (; t < n_rows; t += stride) {
+      const int64_t tn = t + stride;
+      int rn = 0, an = 0, bn = 0;
+      if (tn < n_rows) {
+        rn = rows ? __ldg(rows + tn) : (int)tn;
+        an = __ldg(rowptr + rn);
+        bn = __ldg(rowptr + rn + 1);
+      }
+      epi.emit(r, row_sum_thread<V, XT, Acc>(colidx, values, x, f_col, a, b, keep), es);
+      r = rn;
+      a = an;
+      b = bn;
+    }
   }
   epi.block_done(es, blockIdx.x);
 }
@@ -187,13 +213,17 @@ __global__ void __launch_bounds__(256) csr_group_kernel(const int4 *__restrict__
   const uint64_t keep = policy_keep(x_keep);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / L;
   // every lane of a group sees the same item sequence (same trip count)
-  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L; g < n_items; g += ng) {
-    const int4 it = items[g];
+  int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L;
+  int4 it = g < n_items ? items[g] : make_int4(0, 0, 0, -1);
+  for (; g < n_items; g += ng) {
+    // next item loaded ahead (its latency overlaps this item's sum)
+    const int4 nx = g + ng < n_items ? items[g + ng] : make_int4(0, 0, 0, -1);
     const Acc s = range_sum_group<L, V, XT, Acc>(colidx, values, x, f_col, it.y, it.z, keep);
     if ((threadIdx.x & (L - 1)) == 0) {
       if (it.w < 0) epi.emit(it.x, s, es);
       else partials[it.w] = s;
     }
+    it = nx;
   }
   epi.block_done(es, blockIdx.x);
 }
