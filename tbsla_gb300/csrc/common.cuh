@@ -75,8 +75,12 @@ struct tbsla_matrix {
   int rows_pad = 0;      // ELL: padded row count of the column-major arrays
   int64_t x_extent = 0;  // entries of x the kernels read (max column - f_col + 1)
 
-  // CSR kernel variant: 0 = direct (row bins), 1 = row blocks
+  // CSR kernel variant: 0 = direct (row bins), 1 = row blocks.  COO / SCOO:
+  // 0 = the direct CSR kernels over coo_rowptr, 1 = merge path
   int csr_variant = 0;
+  // COO / SCOO: row pointer of the row-sorted entries (n_row + 1), with the
+  // row bins of the direct kernels built from it
+  int *coo_rowptr = nullptr;
   // fraction of the gathered vector's lines loaded with L2 evict-last
   // priority by the direct CSR kernels (tbsla_matrix_tune)
   float x_keep = 0.6f;

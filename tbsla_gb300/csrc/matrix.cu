@@ -233,7 +233,7 @@ static void free_handle(tbsla_matrix *A) {
                   A->tile_start, A->tile_head_row, A->tile_head_val,
                   A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
                   A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err, A->pr_newid, A->pr_out,
-                  A->transpose_perm};
+                  A->transpose_perm, A->coo_rowptr};
   for (void *p : ptrs) if (p) cudaFree(p);
   if (A->stream) cudaStreamDestroy(A->stream);
   for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -254,6 +254,8 @@ static tbsla_status_t zero_unwritten(const tbsla_matrix *A, void *y, size_t elt,
                                      cudaStream_t s) {
   if (A->n_row <= 0) return TBSLA_OK;
   if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO) {
+    // the direct kernels write every row (empty rows as 0) unless rows are shifted
+    if (A->coo_rowptr && A->csr_variant == 0 && vect_incr == 0 && A->stored > 0) return TBSLA_OK;
     TB_CUDA(cudaMemsetAsync(y, 0, (size_t)A->n_row * elt, s));
     return TBSLA_OK;
   }
@@ -610,6 +612,18 @@ tbsla_status_t tbsla_coo_create(int n_row, int n_col, int f_row, int f_col, int6
   }
   if (st == TBSLA_OK) st = upload_values(A, sv.data(), nnz, stores);
   if (st == TBSLA_OK) st = alloc_carries(A);
+  // the entries are row-sorted: a row pointer makes them CSR for the direct
+  // kernels (cnt[r] is now the end of row r)
+  if (st == TBSLA_OK && n_row > 0) {
+    std::vector<int> rp((size_t)n_row + 1);
+    rp[0] = 0;
+    for (int r = 0; r < n_row; ++r) rp[(size_t)r + 1] = (int)cnt[(size_t)r];
+    st = alloc_n(A, &A->coo_rowptr, (int64_t)n_row + 1);
+    if (st == TBSLA_OK && cudaMemcpy(A->coo_rowptr, rp.data(), ((size_t)n_row + 1) * sizeof(int),
+                                     cudaMemcpyHostToDevice) != cudaSuccess)
+      st = fail(TBSLA_ERR_CUDA, "upload failed");
+    if (st == TBSLA_OK) st = csr_bins(A, rp);
+  }
   if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "sync failed");
   if (st != TBSLA_OK) { free_handle(A); return st; }
   // COO rows are stored relative to f_row: output row = row + vect_incr
@@ -641,6 +655,11 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant) {
   TB_CHECK(A, "matrix is NULL");
   if (A->format == TBSLA_FMT_CSR) {
     TB_CHECK(variant == 0 || variant == 1, "CSR kernel variant %d unknown (0 direct, 1 row blocks)", variant);
+    A->csr_variant = variant;
+    return TBSLA_OK;
+  }
+  if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO) {
+    TB_CHECK(variant == 0 || variant == 1, "COO kernel variant %d unknown (0 direct, 1 merge path)", variant);
     A->csr_variant = variant;
     return TBSLA_OK;
   }
@@ -721,7 +740,14 @@ tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *i
     }
     break;
   case TBSLA_FMT_COO:
-  case TBSLA_FMT_SCOO: k = A->stored > 0 ? 2 : 0; break;
+  case TBSLA_FMT_SCOO:
+    if (A->stored > 0 && A->coo_rowptr && A->csr_variant == 0) {
+      k = (A->n_short > 0) + (A->n_chunk_rows > 0);
+      for (int c = 0; c < kGroupClasses; ++c) k += A->item_class_start[c + 1] > A->item_class_start[c];
+    } else {
+      k = A->stored > 0 ? 2 : 0;
+    }
+    break;
   case TBSLA_FMT_ELL: k = (A->rows > 0 && A->max_col > 0) ? 1 : 0; break;
   default: k = (A->rows > 0 && A->cols > 0) ? 1 : 0; break;
   }

@@ -61,6 +61,53 @@ template <typename Acc> inline Acc *chunk_partials_of(const tbsla_matrix *A);
 template <> inline double *chunk_partials_of<double>(const tbsla_matrix *A) { return A->chunk_partials; }
 template <> inline float *chunk_partials_of<float>(const tbsla_matrix *A) { return A->chunk_partials32; }
 
+// The direct CSR launches (row bins of the handle) over rowptr / colidx:
+// the CSR arrays of a CSR handle, or the derived row pointer of a row-sorted
+// COO handle.
+template <typename V, typename XT, typename Epi>
+tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const int *colidx, const V *vals,
+                                 const XT *x, Epi epi, cudaStream_t s) {
+  using Acc = typename Epi::Acc;
+  KernelTimer kt(A, s);
+  int base = 0;
+  if (A->n_short > 0) {
+    epi.set_part_base(base);
+    base += short_grid(A->n_short, Epi::kReduces);
+    csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
+        A->short_rows, A->n_short, rowptr, colidx, vals, x, A->f_col, A->x_keep, epi);
+  }
+  for (int c = 0; c < kGroupClasses; ++c) {
+    const int first = A->item_class_start[c], count = A->item_class_start[c + 1] - first;
+    if (count == 0) continue;
+    const int grid = group_grid(count, kGroupLanes[c], Epi::kReduces);
+    epi.set_part_base(base);
+    base += grid;
+    const int4 *items = A->warp_items + first;
+    Acc *parts = chunk_partials_of<Acc>(A);
+    switch (kGroupLanes[c]) {
+    case 4:
+      csr_group_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      break;
+    case 8:
+      csr_group_kernel<8, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      break;
+    case 16:
+      csr_group_kernel<16, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      break;
+    default:
+      csr_group_kernel<32, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      break;
+    }
+  }
+  kt.stop();
+  if (A->n_chunk_rows > 0) {
+    epi.set_part_base(base);
+    csr_chunk_fixup_kernel<Epi><<<fixup_grid(A->n_chunk_rows), 128, 0, s>>>(
+        A->chunk_rows, A->n_chunk_rows, chunk_partials_of<Acc>(A), epi);
+  }
+  return TBSLA_OK;
+}
+
 template <typename V, typename XT, typename Epi>
 tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x, Epi epi,
                               cudaStream_t s) {
@@ -68,43 +115,7 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
   switch (A->format) {
   case TBSLA_FMT_CSR:
     if (A->rows > 0 && A->csr_variant == 0) {
-      KernelTimer kt(A, s);
-      int base = 0;
-      if (A->n_short > 0) {
-        epi.set_part_base(base);
-        base += short_grid(A->n_short, Epi::kReduces);
-        csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
-            A->short_rows, A->n_short, A->idx0, A->idx1, vals, x, A->f_col, A->x_keep, epi);
-      }
-      for (int c = 0; c < kGroupClasses; ++c) {
-        const int first = A->item_class_start[c], count = A->item_class_start[c + 1] - first;
-        if (count == 0) continue;
-        const int grid = group_grid(count, kGroupLanes[c], Epi::kReduces);
-        epi.set_part_base(base);
-        base += grid;
-        const int4 *items = A->warp_items + first;
-        Acc *parts = chunk_partials_of<Acc>(A);
-        switch (kGroupLanes[c]) {
-        case 4:
-          csr_group_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
-          break;
-        case 8:
-          csr_group_kernel<8, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
-          break;
-        case 16:
-          csr_group_kernel<16, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
-          break;
-        default:
-          csr_group_kernel<32, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, A->idx1, vals, x, A->f_col, A->x_keep, parts, epi);
-          break;
-        }
-      }
-      kt.stop();
-      if (A->n_chunk_rows > 0) {
-        epi.set_part_base(base);
-        csr_chunk_fixup_kernel<Epi><<<fixup_grid(A->n_chunk_rows), 128, 0, s>>>(
-            A->chunk_rows, A->n_chunk_rows, chunk_partials_of<Acc>(A), epi);
-      }
+      TB_TRY(launch_csr_direct<V, XT>(A, A->idx0, A->idx1, vals, x, epi, s));
     } else if (A->rows > 0) {
       const size_t smem = csr_rows_setup<V, XT, Epi>();
       KernelTimer kt(A, s);
@@ -118,7 +129,9 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
     break;
   case TBSLA_FMT_COO:
   case TBSLA_FMT_SCOO:
-    if (A->stored > 0) {
+    if (A->stored > 0 && A->coo_rowptr && A->csr_variant == 0) {
+      TB_TRY(launch_csr_direct<V, XT>(A, A->coo_rowptr, A->idx1, vals, x, epi, s));
+    } else if (A->stored > 0) {
       KernelTimer kt(A, s);
       coo_merge_kernel<kMergeThreads, kMergeItems, V, XT, Epi><<<A->num_tiles, kMergeThreads, 0, s>>>(
           A->idx0, A->idx1, vals, x, A->f_col, A->stored, carry_of<Acc>(A), epi);

@@ -294,3 +294,26 @@ def test_invalid_arguments_are_reported(gpu):
     m = gpu.DeviceMatrix.csr(3, 3, [0, 1, 2, 3], [0, 1, 2], [1.0, 1.0, 1.0])
     with pytest.raises(gpu.TbslaError):
         m.spmv_ex(gpu.F32, gpu.F64, 0, gpu.F64, 0)  # no F32 store
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_coo_variants(gpu, orc, variant):
+    """COO / SCOO through the direct CSR kernels over the derived row pointer
+    (variant 0) and through the merge path (variant 1): unsorted triplets
+    with repeated entries, empty rows, a hub row, SCOO offsets, row shifts."""
+    rng = np.random.default_rng(17 + variant)
+    n_row, n_col, nnz = 4000, 3000, 50000
+    row = rng.integers(0, n_row, nnz).astype(np.int32)
+    row[:9000] = 7  # one row longer than the chunk size of the direct kernels
+    row[row % 13 == 0] = 1  # rows multiple of 13 stay empty
+    col = rng.integers(0, n_col, nnz).astype(np.int32)
+    val = rng.standard_normal(nnz)
+    for (f_row, f_col) in ((0, 0), (100, 50)):
+        m = gpu.DeviceMatrix.coo(n_row, n_col, row + f_row, col + f_col, val, f_row=f_row, f_col=f_col)
+        m.set_variant(variant)
+        o = orc.from_arrays("COO", n_row, n_col, val, row, col)
+        so = orc.from_arrays("COO", n_row, n_col, np.abs(val), row, col)
+        x = rng.uniform(-1, 1, n_col)
+        for incr in (0, 3, -2):
+            assert_close(m.spmv_host(x, incr), o.spmv(x, incr), so.spmv(np.abs(x), incr), RTOL64,
+                         f"coo variant {variant} offsets {f_row},{f_col} shift {incr}")
