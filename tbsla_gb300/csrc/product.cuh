@@ -143,8 +143,12 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
     if (A->rows > 0 && A->max_col > 0) {
       const int threads = (A->rows + 3) / 4;
       KernelTimer kt(A, s);
-      ell_kernel<V, XT, Epi><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                 A->rows_pad, A->max_col, A->x_keep, epi);
+      if (A->x_extent * (int64_t)sizeof(XT) <= (64ll << 20))
+        ell_kernel<V, XT, Epi, true><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                           A->rows_pad, A->max_col, A->x_keep, epi);
+      else
+        ell_kernel<V, XT, Epi, false><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                            A->rows_pad, A->max_col, A->x_keep, epi);
       kt.stop();
     }
     break;
