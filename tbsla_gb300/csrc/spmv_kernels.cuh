@@ -254,7 +254,7 @@ template <typename V> struct Vec4 { V v[4]; };
 // x is larger than L2, where evict-first row data measured slower (ELL FP64
 // cqmat 2^24: 3.6 vs 4.0 TB/s; 2^22: 5.95 vs 5.68 TB/s).
 template <bool CS, typename T> __device__ __forceinline__ T ld_row(const T *p) {
-  if constexpr (CS) return ld_row<CS>(p);
+  if constexpr (CS) return __ldcs(p);
   else return __ldg(p);
 }
 
