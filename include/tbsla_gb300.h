@@ -127,6 +127,15 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *   TBSLA_TUNE_X_L2_KEEP  fraction in [0, 1] of the gathered vector x that the
  *                         CSR product loads with L2 evict-last priority (the
  *                         rest with normal priority); default 0.6.
+ *   TBSLA_TUNE_X_L2_RANGE 1: the kept fraction is the leading part of x by
+ *                         address (the same lines on every load: an L2
+ *                         range policy); 0 (default): a fraction of the
+ *                         lines touched.
+ *   TBSLA_TUNE_CSR_STAGE  1: when every row holds at most 32 entries, the
+ *                         CSR product stages each 32-row tile's entries in
+ *                         shared memory with coalesced loads and sums each
+ *                         row from there (one thread per row); 0: rows are
+ *                         read straight from global memory.
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)
@@ -134,7 +143,12 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         vertices, is not banded and its top tenth of
  *                         vertices holds half of the entries.  Results are
  *                         returned in the original labels. */
-typedef enum { TBSLA_TUNE_X_L2_KEEP = 0, TBSLA_TUNE_PR_RELABEL = 1 } tbsla_tune_knob_t;
+typedef enum {
+  TBSLA_TUNE_X_L2_KEEP = 0,
+  TBSLA_TUNE_PR_RELABEL = 1,
+  TBSLA_TUNE_X_L2_RANGE = 2,
+  TBSLA_TUNE_CSR_STAGE = 3
+} tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
 
@@ -248,10 +262,12 @@ tbsla_status_t tbsla_batch_destroy(tbsla_batch_t *B);
 typedef struct {
   int candidates;   /* candidates timed                         */
   float best_ms;    /* time of the kept one                     */
-  int choice;       /* spmv: kernel variant; batch: blocks per SM; ppr: tile */
+  int choice;       /* spmv: 0 direct, 1 row blocks, 2 staged short rows;
+                       batch: blocks per SM; ppr: tile */
   double value;     /* spmv: x L2-keep fraction; otherwise = choice */
 } tbsla_autotune_result_t;
-/* CSR kernel variant and TBSLA_TUNE_X_L2_KEEP for the `store` product */
+/* CSR kernel variant, TBSLA_TUNE_CSR_STAGE and TBSLA_TUNE_X_L2_KEEP for the
+ * `store` product (COO / SCOO: the staged kernel and the keep fraction) */
 tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_autotune_result_t *res);
 /* persistent grid of a bound batch */
 tbsla_status_t tbsla_autotune_batch(tbsla_batch_t *B, tbsla_autotune_result_t *res);

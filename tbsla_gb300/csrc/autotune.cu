@@ -3,8 +3,9 @@
 // Each tuner times its candidates with CUDA events on a private stream
 // (after one untimed run of each, so first-touch costs do not count), keeps
 // the fastest, and stores it where the library reads it: the CSR product's
-// kernel variant and x L2-keep fraction (tbsla_matrix_set_variant /
-// TBSLA_TUNE_X_L2_KEEP), the persistent grid of a matrix batch
+// kernel variant, staged short-row kernel and x L2-keep fraction
+// (tbsla_matrix_set_variant / TBSLA_TUNE_CSR_STAGE / TBSLA_TUNE_X_L2_KEEP),
+// the persistent grid of a matrix batch
 // (tbsla_batch_tune), the tile width of batched PageRank (used when
 // tbsla_ppr_batched is called with tile 0).  Results never depend on these
 // choices, only times do.
@@ -65,15 +66,20 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   cudaStream_t s;
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   const float keeps[] = {0.0f, 0.3f, 0.6f, 1.0f};
-  const int variants = A->format == TBSLA_FMT_CSR ? 2 : 1;
+  // kernels: 0 direct, 1 row blocks (CSR), 2 direct with the staged
+  // short-row kernel (every row at most 32 entries)
+  const bool csr = A->format == TBSLA_FMT_CSR;
   float best = 1e30f;
-  int best_v = A->csr_variant;
+  int best_v = A->csr_variant == 0 && A->stage_mode > 0 ? 2 : A->csr_variant;
   float best_k = A->x_keep;
   tbsla_status_t st = TBSLA_OK;
   int tried = 0;
-  for (int v = 0; v < variants && st == TBSLA_OK; ++v)
+  for (int v = 0; v < 3 && st == TBSLA_OK; ++v) {
+    if (v == 1 && !csr) continue;
+    if (v == 2 && A->stage_cap == 0) continue;
     for (float k : keeps) {
-      if (A->format == TBSLA_FMT_CSR) A->csr_variant = v;
+      if (csr) A->csr_variant = v == 1 ? 1 : 0;
+      A->stage_mode = v == 2 ? 1 : 0;
       A->x_keep = k;
       float ms = 0;
       st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
@@ -82,11 +88,14 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
       if (ms < best) { best = ms; best_v = v; best_k = k; }
       if (v == 1) break;  // the row-block kernel does not read x_keep
     }
+  }
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
   cudaFree(x);
   cudaFree(y);
-  A->csr_variant = best_v;
+  if (csr) A->csr_variant = best_v == 1 ? 1 : 0;
+  A->stage_mode = best_v == 2 ? 1 : 0;
+  if (A->pr_relabel) A->pr_relabel->stage_mode = A->stage_mode;
   A->x_keep = best_k;
   if (res) {
     res->candidates = tried;

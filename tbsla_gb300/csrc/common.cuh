@@ -84,10 +84,16 @@ struct tbsla_matrix {
   // fraction of the gathered vector's lines loaded with L2 evict-last
   // priority by the direct CSR kernels (tbsla_matrix_tune)
   float x_keep = 0.6f;
+  // 1: the kept fraction is the leading part of x by address (range policy)
+  int x_keep_range = 0;
   // CSR direct bins (csr_direct.cuh): short rows (NULL = all rows), warp
   // items (long rows and chunks of huge rows), huge rows, chunk partials
   int *short_rows = nullptr;
   int n_short = 0;
+  // all rows short: shared-memory slots per warp of the staged kernel (the
+  // entries of the largest 32-row tile, a multiple of 16); 0 otherwise
+  int stage_cap = 0;
+  int stage_mode = 0;  // staged kernel: 1 on, 0 off (tbsla_matrix_tune)
   int4 *warp_items = nullptr;
   int n_warp_items = 0;
   int item_class_start[5] = {0, 0, 0, 0, 0};  // items of length class c: [start[c], start[c+1])
@@ -212,6 +218,23 @@ __device__ __forceinline__ uint64_t policy_keep(float f) {
   return p;
 }
 
+// What the kernels keep of the gathered vector: a fraction of its lines
+// (fractional policy), or, when `range` is the vector's size in bytes, the
+// first `frac` of its addresses (range policy: the same lines every time).
+struct XKeep {
+  float frac;
+  uint32_t range;
+};
+__device__ __forceinline__ uint64_t policy_keep(XKeep k, const void *x) {
+  if (k.range == 0 || k.frac <= 0.f) return policy_keep(k.frac);
+  const uint32_t primary = (uint32_t)fminf((float)k.range, k.frac * (float)k.range);
+  uint64_t p;
+  asm volatile("createpolicy.range.global.L2::evict_last.L2::evict_unchanged.b64 %0, [%1], %2, %3;"
+               : "=l"(p)
+               : "l"(x), "r"(primary), "r"(k.range));
+  return p;
+}
+
 __device__ __forceinline__ uint64_t policy_evict_first() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -235,16 +258,21 @@ __device__ __forceinline__ void cp_async(void *smem, const void *gmem, uint64_t 
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most N of this thread's committed groups are pending
+template <int N> __device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 template <typename T> __device__ __forceinline__ T ld_keep(const T *p, uint64_t pol);
 template <> __device__ __forceinline__ double ld_keep<double>(const double *p, uint64_t pol) {
   double v;
-  asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
   return v;
 }
 template <> __device__ __forceinline__ float ld_keep<float>(const float *p, uint64_t pol) {
   float v;
-  asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
   return v;
 }
 

@@ -137,12 +137,12 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
                                                        const int *__restrict__ rowptr,
                                                        const int *__restrict__ colidx,
                                                        const V *__restrict__ values,
-                                                       const XT *__restrict__ x, int f_col, float x_keep,
+                                                       const XT *__restrict__ x, int f_col, XKeep x_keep,
                                                        Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   typename Epi::State es{};
-  const uint64_t keep = policy_keep(x_keep);
+  const uint64_t keep = policy_keep(x_keep, x);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if constexpr (!Epi::kReduces) {
@@ -205,12 +205,12 @@ template <int L, typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_group_kernel(const int4 *__restrict__ items, int n_items,
                                                        const int *__restrict__ colidx,
                                                        const V *__restrict__ values,
-                                                       const XT *__restrict__ x, int f_col, float x_keep,
+                                                       const XT *__restrict__ x, int f_col, XKeep x_keep,
                                                        typename Epi::Acc *__restrict__ partials, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   typename Epi::State es{};
-  const uint64_t keep = policy_keep(x_keep);
+  const uint64_t keep = policy_keep(x_keep, x);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / L;
   // every lane of a group sees the same item sequence (same trip count)
   int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / L;
@@ -224,6 +224,126 @@ __global__ void __launch_bounds__(256) csr_group_kernel(const int4 *__restrict__
       else partials[it.w] = s;
     }
     it = nx;
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
+// ---------------------------------------------------------------- staged
+// Matrices whose rows are all short (<= kShortRow entries).  A warp takes
+// tiles of 32 consecutive rows; a tile's entries are contiguous, and the warp
+// copies them into its slice of shared memory with lane-per-entry copies
+// (each line of row data read by one instruction, evict-first in L2 so that
+// the streamed matrix leaves L2 to x).  Then each lane sums its own row from
+// shared memory in stored order, one FMA per entry (the direct kernel's
+// arithmetic: results are bit-identical), gathering x with the kept-fraction
+// policy.  Slots are XOR-swizzled within groups of 16 entries, so lanes
+// reading rows of 16 entries hit distinct banks.  Warps work independently;
+// the block meets only in the epilogue's reduction.  (Per-element cp.async
+// copies into two buffers per warp, overlapping the next tile's copies with
+// the current sum, measured 1.5x slower than these register copies.)
+constexpr int kStageWarps = 8;
+constexpr int kStageBatch = 8;                // loads in flight per lane
+constexpr int kStageCapMax = 32 * kShortRow;  // a tile's entries when every row is short
+
+template <typename T> __device__ __forceinline__ T ld_first(const T *p, uint64_t pol);
+template <> __device__ __forceinline__ double ld_first<double>(const double *p, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <> __device__ __forceinline__ float ld_first<float>(const float *p, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <> __device__ __forceinline__ int ld_first<int>(const int *p, uint64_t pol) {
+  int v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+template <> __device__ __forceinline__ __nv_bfloat16 ld_first<__nv_bfloat16>(const __nv_bfloat16 *p, uint64_t pol) {
+  unsigned short v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  return __ushort_as_bfloat16(v);
+}
+
+__device__ __forceinline__ int stage_swz(int k) { return k ^ ((k >> 4) & 15); }
+
+// dynamic shared memory of csr_stage_kernel for value type V and `cap` slots
+template <typename V> constexpr size_t csr_stage_smem(int cap) {
+  return (size_t)kStageWarps * cap * (sizeof(V) + sizeof(int));
+}
+
+// lane bounds of tile t: row r0+lane spans [lo, hi); lanes past the matrix
+// (or a tile past the end) see empty rows
+__device__ __forceinline__ void stage_bounds(const int *__restrict__ rowptr, int rows, int n_tiles, int t, int lane,
+                                             int &lo, int &hi) {
+  lo = hi = 0;
+  if (t < n_tiles) {
+    const int r0 = t << 5, nr = min(32, rows - r0);
+    lo = __ldg(rowptr + r0 + min(lane, nr));
+    hi = __ldg(rowptr + r0 + min(lane + 1, nr));
+  }
+}
+
+template <typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc stage_row_sum(const V *sv, const int *sc, int a, int b, const XT *__restrict__ x,
+                                             int f_col, uint64_t keep) {
+  Acc acc = 0;
+  #pragma unroll 8
+  for (int k = a; k < b; ++k) {
+    const int sk = stage_swz(k);
+    acc = fma_acc(to_acc(sv[sk], Acc()), to_acc(ld_keep(x + (sc[sk] - f_col), keep), Acc()), acc);
+  }
+  return acc;
+}
+
+template <typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(kStageWarps * 32) csr_stage_kernel(int rows, const int *__restrict__ rowptr,
+                                                                    const int *__restrict__ colidx,
+                                                                    const V *__restrict__ values,
+                                                                    const XT *__restrict__ x, int f_col,
+                                                                    XKeep x_keep, int cap, Epi epi) {
+  using Acc = typename Epi::Acc;
+  extern __shared__ __align__(16) unsigned char stage_smem[];
+  if (!epi.active()) return;
+  typename Epi::State es{};
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  V *sv = reinterpret_cast<V *>(stage_smem) + (size_t)wib * cap;
+  int *sc = reinterpret_cast<int *>(stage_smem + (size_t)kStageWarps * cap * sizeof(V)) + (size_t)wib * cap;
+  const uint64_t keep = policy_keep(x_keep, x), first = policy_evict_first();
+  const int n_tiles = (rows + 31) >> 5;
+  const int nw = gridDim.x * kStageWarps;
+  int t = blockIdx.x * kStageWarps + wib;
+  for (; t < n_tiles; t += nw) {
+    int lo, hi;
+    stage_bounds(rowptr, rows, n_tiles, t, lane, lo, hi);
+    const int e0 = __shfl_sync(0xffffffffu, lo, 0), e1 = __shfl_sync(0xffffffffu, hi, 31);
+    const int n = e1 - e0;  // <= cap by construction
+    for (int k0 = 0; k0 < n; k0 += 32 * kStageBatch) {
+      V v[kStageBatch];
+      int c[kStageBatch];
+      #pragma unroll
+      for (int u = 0; u < kStageBatch; ++u) {
+        const int k = k0 + u * 32 + lane;
+        if (k < n) {
+          v[u] = ld_first(values + e0 + k, first);
+          c[u] = ld_first(colidx + e0 + k, first);
+        }
+      }
+      #pragma unroll
+      for (int u = 0; u < kStageBatch; ++u) {
+        const int k = k0 + u * 32 + lane;
+        if (k < n) {
+          sv[stage_swz(k)] = v[u];
+          sc[stage_swz(k)] = c[u];
+        }
+      }
+    }
+    __syncwarp();
+    const Acc acc = stage_row_sum<V, XT, Acc>(sv, sc, lo - e0, hi - e0, x, f_col, keep);
+    if ((t << 5) + lane < rows) epi.emit((t << 5) + lane, acc, es);
+    __syncwarp();  // the next tile's copies overwrite the slots
   }
   epi.block_done(es, blockIdx.x);
 }

@@ -444,6 +444,14 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     }
     A->item_class_start[kGroupClasses] = (int)items.size();
     A->n_short = (int)shorts.size();
+    // staged kernel (all rows short): entries of the largest 32-row tile,
+    // rounded up to the 16-entry swizzle group
+    A->stage_cap = 0;
+    if (all_short && rows > 0) {
+      int cap = 0;
+      for (int r = 0; r < rows; r += 32) cap = std::max(cap, rp[std::min(r + 32, rows)] - rp[r]);
+      A->stage_cap = std::max(16, (cap + 15) / 16 * 16);
+    }
     if (!all_short && !shorts.empty()) {
       TB_TRY(alloc_n(A, &A->short_rows, (int64_t)shorts.size()));
       TB_CUDA(cudaMemcpy(A->short_rows, shorts.data(), shorts.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -679,6 +687,17 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
   case TBSLA_TUNE_PR_RELABEL:
     TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0, "PageRank relabel mode %g not -1, 0 or 1", value);
     A->pr_relabel_mode = (int)value;
+    return TBSLA_OK;
+  case TBSLA_TUNE_CSR_STAGE:
+    TB_CHECK(value == 0.0 || value == 1.0, "staged kernel mode %g not 0 or 1", value);
+    A->stage_mode = (int)value;
+    if (A->pr_relabel) A->pr_relabel->stage_mode = (int)value;
+    return TBSLA_OK;
+  case TBSLA_TUNE_X_L2_RANGE:
+    TB_CHECK(value == 0.0 || value == 1.0, "x L2 range mode %g not 0 or 1", value);
+    A->x_keep_range = (int)value;
+    if (A->pr_relabel) A->pr_relabel->x_keep_range = (int)value;
+    if (A->transpose) A->transpose->x_keep_range = (int)value;
     return TBSLA_OK;
   default:
     return fail(TBSLA_ERR_INVALID_ARG, "unknown tuning knob %d", knob);

@@ -80,8 +80,10 @@ __device__ __forceinline__ void block_reduce3(double a, double b, double c, bool
 template <typename YT, typename AccT> struct PrEpi {
   using Acc = AccT;
   static constexpr bool kReduces = true;  // per-block partials: capped grids
+  // per-thread sums in the accumulator type: FP64 sweeps sum in FP64, the
+  // FP32 inner sweeps of the mixed solve in FP32 (no FP64 operation per row)
   struct State {
-    double a = 0, b = 0, c = 0;
+    AccT a = 0, b = 0, c = 0;
   };
   YT *y;
   const YT *xold;               // previous iterate (residual)
@@ -100,10 +102,14 @@ template <typename YT, typename AccT> struct PrEpi {
     if (row < 0 || row >= n) return;
     double val;
     const double beta = *betap;
-    if (mode == kSweepInner) {
+    if constexpr (std::is_same<AccT, float>::value) {
+      // inner sweep (kSweepInner): e' = beta*G~e + add + r in FP32
       const float f = __fmaf_rn((float)beta, (float)v, (float)*add) + (float)rvec[row];
-      val = f;
-      st.a += fabs(val - (double)xold[row]);
+      st.a += fabsf(f - (float)xold[row]);
+      if (dmask && dmask[row]) st.b += f;
+      st.c += f;
+      __stcs(y + row, (YT)f);
+      return;
     } else {
       const double t = mode == kSweepTele ? *add * tvec[row]
                        : (mode == kSweepRef && tmask) ? (tmask[row] ? *add : 0.0) : *add;
@@ -118,7 +124,7 @@ template <typename YT, typename AccT> struct PrEpi {
     __stcs(y + row, (YT)val);
   }
   __device__ __forceinline__ void block_done(State &st, int blk) const {
-    block_reduce3(st.a, st.b, st.c, mode == kSweepRef, partials, part_base + blk);
+    block_reduce3((double)st.a, (double)st.b, (double)st.c, mode == kSweepRef, partials, part_base + blk);
   }
   __device__ __forceinline__ void fixup_done(State &st, int blk) const { block_done(st, blk); }
 };

@@ -61,6 +61,33 @@ template <typename Acc> inline Acc *chunk_partials_of(const tbsla_matrix *A);
 template <> inline double *chunk_partials_of<double>(const tbsla_matrix *A) { return A->chunk_partials; }
 template <> inline float *chunk_partials_of<float>(const tbsla_matrix *A) { return A->chunk_partials32; }
 
+// The handle's L2 policy on the gathered vector (x of type XT).  The range
+// form needs the vector's bytes in 32 bits; larger vectors keep a fraction.
+template <typename XT> inline XKeep xkeep_of(const tbsla_matrix *A) {
+  XKeep k{A->x_keep, 0u};
+  const int64_t bytes = A->x_extent * (int64_t)sizeof(XT);
+  if (A->x_keep_range && bytes > 0 && bytes <= (int64_t)0xffffffffll) k.range = (uint32_t)bytes;
+  return k;
+}
+
+// The staged kernel applies when every row is short (stage_cap > 0) and the
+// handle's stage mode (tbsla_matrix_tune) is on.
+inline bool stage_on(const tbsla_matrix *A) {
+  return A->stage_cap > 0 && A->short_rows == nullptr && A->stage_mode > 0 &&
+         A->stage_cap <= kStageCapMax;
+}
+// dynamic shared memory of csr_stage_kernel (the attribute is raised once per
+// instantiation to the largest capacity)
+template <typename V, typename XT, typename Epi> size_t csr_stage_setup(int cap) {
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(csr_stage_kernel<V, XT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)csr_stage_smem<V>(kStageCapMax));
+    done = true;
+  }
+  return csr_stage_smem<V>(cap);
+}
+
 // The direct CSR launches (row bins of the handle) over rowptr / colidx:
 // the CSR arrays of a CSR handle, or the derived row pointer of a row-sorted
 // COO handle.
@@ -70,11 +97,22 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
   using Acc = typename Epi::Acc;
   KernelTimer kt(A, s);
   int base = 0;
-  if (A->n_short > 0) {
+  if (A->n_short > 0 && stage_on(A)) {
+    // all rows short: the staged kernel (reducing epilogues: the same grid as
+    // the short-row kernel, so that every partial slot is written)
+    const size_t smem = csr_stage_setup<V, XT, Epi>(A->stage_cap);
+    const int tiles = (A->n_short + 31) / 32;
+    const int grid = Epi::kReduces ? short_grid(A->n_short, true)
+                                   : std::max(1, std::min((tiles + kStageWarps - 1) / kStageWarps, kStrideBlocks));
+    epi.set_part_base(base);
+    base += short_grid(A->n_short, Epi::kReduces);
+    csr_stage_kernel<V, XT, Epi><<<grid, kStageWarps * 32, smem, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
+                                                                     xkeep_of<XT>(A), A->stage_cap, epi);
+  } else if (A->n_short > 0) {
     epi.set_part_base(base);
     base += short_grid(A->n_short, Epi::kReduces);
     csr_short_kernel<V, XT, Epi><<<short_grid(A->n_short, Epi::kReduces), 256, 0, s>>>(
-        A->short_rows, A->n_short, rowptr, colidx, vals, x, A->f_col, A->x_keep, epi);
+        A->short_rows, A->n_short, rowptr, colidx, vals, x, A->f_col, xkeep_of<XT>(A), epi);
   }
   for (int c = 0; c < kGroupClasses; ++c) {
     const int first = A->item_class_start[c], count = A->item_class_start[c + 1] - first;
@@ -86,16 +124,16 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
     Acc *parts = chunk_partials_of<Acc>(A);
     switch (kGroupLanes[c]) {
     case 4:
-      csr_group_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      csr_group_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, xkeep_of<XT>(A), parts, epi);
       break;
     case 8:
-      csr_group_kernel<8, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      csr_group_kernel<8, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, xkeep_of<XT>(A), parts, epi);
       break;
     case 16:
-      csr_group_kernel<16, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      csr_group_kernel<16, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, xkeep_of<XT>(A), parts, epi);
       break;
     default:
-      csr_group_kernel<32, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, A->x_keep, parts, epi);
+      csr_group_kernel<32, V, XT, Epi><<<grid, 256, 0, s>>>(items, count, colidx, vals, x, A->f_col, xkeep_of<XT>(A), parts, epi);
       break;
     }
   }
@@ -145,10 +183,10 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
       KernelTimer kt(A, s);
       if (A->x_extent * (int64_t)sizeof(XT) <= (64ll << 20))
         ell_kernel<V, XT, Epi, true><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                           A->rows_pad, A->max_col, A->x_keep, epi);
+                                                                           A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
       else
         ell_kernel<V, XT, Epi, false><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                            A->rows_pad, A->max_col, A->x_keep, epi);
+                                                                            A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
       kt.stop();
     }
     break;

@@ -281,13 +281,13 @@ template <typename V, typename XT, typename Epi, bool CS>
 __global__ void __launch_bounds__(256) ell_kernel(const int *__restrict__ cols,
                                                   const V *__restrict__ vals,
                                                   const XT *__restrict__ x, int f_col, int rows,
-                                                  int rows_pad, int max_col, float x_keep, Epi epi) {
+                                                  int rows_pad, int max_col, XKeep x_keep, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
   const int r0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
   typename Epi::State es{};
   if (r0 < rows) {
-    const uint64_t keep = policy_keep(x_keep);
+    const uint64_t keep = policy_keep(x_keep, x);
     Acc a[4] = {0, 0, 0, 0};
     #pragma unroll 4
     for (int s = 0; s < max_col; ++s) {

@@ -110,7 +110,7 @@ def test_autotuners_keep_results(gpu, orc):
     x = np.random.default_rng(0).uniform(-1, 1, 1 << 12)
     before = A.spmv_host(x)
     r = A.autotune_spmv(gpu.F64)
-    assert r.candidates >= 2 and r.best_ms > 0 and r.choice in (0, 1) and 0.0 <= r.value <= 1.0
+    assert r.candidates >= 2 and r.best_ms > 0 and r.choice in (0, 1, 2) and 0.0 <= r.value <= 1.0
     after = A.spmv_host(x)
     assert np.allclose(after, before, rtol=1e-13, atol=1e-15)
     sets = [[i * 37 % 4096] for i in range(48)]

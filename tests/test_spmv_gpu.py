@@ -319,3 +319,49 @@ def test_coo_variants(gpu, orc, variant):
         for incr in (0, 3, -2):
             assert_close(m.spmv_host(x, incr), o.spmv(x, incr), so.spmv(np.abs(x), incr), RTOL64,
                          f"coo variant {variant} offsets {f_row},{f_col} shift {incr}")
+
+
+def test_csr_staged_kernel(gpu, orc):
+    """The staged kernel (every row at most 32 entries, 32-row tiles copied to
+    shared memory) sums each row in stored order with one FMA per entry, as
+    the direct kernel does: results are bit-identical to it and within the
+    FP64 bound of the oracle.  Uniform, ragged (empty rows, row counts that
+    are not a multiple of 32), full (32-entry rows: the largest tile) and
+    reduced-precision stores; a_axpx and the PageRank sweep epilogue."""
+    rng = np.random.default_rng(31)
+    cases = [(20000, 20000, np.full(20000, 16)), (20011, 5000, rng.integers(0, 33, 20011)),
+             (4133, 70000, np.full(4133, 32)), (33, 40, rng.integers(0, 4, 33)), (1, 7, np.array([5]))]
+    for (nr, nc, lens) in cases:
+        rp, ci, va = random_csr(rng, nr, nc, lens)
+        x = rng.uniform(-1, 1, nc)
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
+        y0 = m.spmv_host(x)
+        m.tune(gpu.TUNE_CSR_STAGE, 1)
+        y1 = m.spmv_host(x)
+        assert np.array_equal(y0, y1), f"staged {nr}x{nc}: not bit-identical"
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+        assert_close(y1, o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"staged {nr}x{nc}")
+        for store in (gpu.F32, gpu.BF16):
+            outs = []
+            for mode in (0, 1):
+                m.tune(gpu.TUNE_CSR_STAGE, mode)
+                xs = Dev.of(gpu, x.astype(np.float32))
+                ys = Dev(gpu, nr, np.float32)
+                m.spmv_ex(store, gpu.F32, xs.ptr, gpu.F32, ys.ptr)
+                outs.append(ys.get())
+            assert np.array_equal(outs[0], outs[1]), f"staged store {store} {nr}x{nc}"
+        if nr == nc:
+            m.tune(gpu.TUNE_CSR_STAGE, 0)
+            r0 = m.a_axpx_host(x)
+            m.tune(gpu.TUNE_CSR_STAGE, 1)
+            assert np.array_equal(r0, m.a_axpx_host(x)), "staged a_axpx"
+    # PageRank sweeps (reducing epilogue) on a column-stochastic cqmat
+    g = gpu.generate("CSR", "cqmat_stochastic", 50000, 50000, 12, 0.1, 2)
+    m = gpu.DeviceMatrix.from_generated(g)
+    x0, r0 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
+    m.tune(gpu.TUNE_CSR_STAGE, 1)
+    x1, r1 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
+    # the per-block partial sums group rows differently: equal to rounding
+    assert abs(r0.iterations - r1.iterations) <= 1 and r1.converged
+    assert float(np.abs(x0 - x1).sum()) <= 1e-11
