@@ -370,6 +370,21 @@ tbsla_status_t tbsla_personalized_pagerank_host(tbsla_matrix_t *A, const tbsla_p
  * equal pairs in input order (the host conversion's arrays, bit for bit).
  * stores: the value stores of the new handle (the COO handle needs F64). */
 tbsla_status_t tbsla_coo_to_csr(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+/* COO / SCOO handle -> ELL handle on the device: MatrixELL(const MatrixCOO&)
+ * (MatrixELL.cpp:12-53): max_col = the longest row, row i's entries in
+ * (row, column) order in slots 0..len-1, padding slots column 0 / value 0.
+ * The handle equals tbsla_ell_create on the host conversion's arrays. */
+tbsla_status_t tbsla_coo_to_ell(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+/* COO / SCOO handle -> DENSE handle (n_row x n_col) on the device:
+ * MatrixDENSE(const MatrixCOO&) (MatrixDENSE.cpp:11-28), repeated (row,
+ * column) pairs added to 0 in input order.  Stored columns must lie below
+ * n_col (the reference indexes the dense row with them). */
+tbsla_status_t tbsla_coo_to_dense(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+/* host copies in the reference's layouts: ELL columns / values row-major
+ * (rows x max_col, MatrixELL::get_columns / get_values); DENSE values
+ * (rows x ln_col).  Either pointer may be NULL. */
+tbsla_status_t tbsla_ell_download(const tbsla_matrix_t *A, int *columns, double *values);
+tbsla_status_t tbsla_dense_download(const tbsla_matrix_t *A, double *values);
 
 /* ---------------------------------------------------------------- files */
 /* A handle (F64 store) from a file in the reference's binary matrix layout

@@ -129,6 +129,10 @@ def lib() -> C.CDLL:
         "tbsla_matrix_read_file": ([C.c_char_p, C.c_int, C.c_int64, C.POINTER(P)], st),
         "tbsla_matrix_read_mm": ([C.c_char_p, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_csr": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_coo_to_ell": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_coo_to_dense": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_ell_download": ([P, _vp, _vp], st),
+        "tbsla_dense_download": ([P, _vp], st),
         "tbsla_dense_spmm": ([P, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp], st),
         "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
         "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
@@ -409,6 +413,33 @@ class DeviceMatrix:
         h = _vp()
         check(lib().tbsla_coo_to_csr(self.h, stores, C.byref(h)))
         return DeviceMatrix(h)
+
+    def to_ell(self, stores=STORE_F64):
+        """ELL handle converted on the device from this COO / SCOO handle."""
+        h = _vp()
+        check(lib().tbsla_coo_to_ell(self.h, stores, C.byref(h)))
+        return DeviceMatrix(h)
+
+    def to_dense(self, stores=STORE_F64):
+        """DENSE handle converted on the device from this COO / SCOO handle."""
+        h = _vp()
+        check(lib().tbsla_coo_to_dense(self.h, stores, C.byref(h)))
+        return DeviceMatrix(h)
+
+    def ell_download(self):
+        """(columns, values) of an ELL handle, row-major rows x max_col."""
+        i = self.info()
+        cols = np.zeros(max(i.rows * i.max_col, 1), np.int32)
+        vals = np.zeros(max(i.rows * i.max_col, 1), np.float64)
+        check(lib().tbsla_ell_download(self.h, _ptr(cols), _ptr(vals)))
+        return cols[: i.rows * i.max_col], vals[: i.rows * i.max_col]
+
+    def dense_download(self):
+        """values of a DENSE handle (stored entries, row-major)."""
+        i = self.info()
+        vals = np.zeros(max(i.stored, 1), np.float64)
+        check(lib().tbsla_dense_download(self.h, _ptr(vals)))
+        return vals[: i.stored]
 
     @classmethod
     def read_file(cls, path: str, fmt: str, seek: int = 0):

@@ -138,3 +138,163 @@ extern "C" tbsla_status_t tbsla_coo_to_csr(const tbsla_matrix_t *C, int stores, 
   *out = A;
   return TBSLA_OK;
 }
+
+// ------------------------------------------------------------------ ELL / DENSE
+// MatrixELL(const MatrixCOO&) (src/cpp/matrix/MatrixELL.cpp:12-53) and
+// MatrixDENSE(const MatrixCOO&) (src/cpp/matrix/MatrixDENSE.cpp:11-28) on the
+// device, through the (row, column)-sorted CSR arrays of tbsla_coo_to_csr:
+// ELL row i holds its entries in that order in slots 0..len-1, padding slots
+// column 0 and value 0 (rows padded to a multiple of four: column f_col, as
+// tbsla_ell_create pads them); DENSE adds the entries of a (row, column) pair
+// to 0 in input order, as the reference's += loop does.  The results equal
+// tbsla_ell_create / tbsla_dense_create on the host conversion's arrays.
+namespace tbsla {
+namespace {
+
+// slot-major ELL arrays from sorted CSR arrays (one thread per padded row)
+__global__ void ell_fill_kernel(const int *__restrict__ rp, const int *__restrict__ ci,
+                                const double *__restrict__ va, int rows, int rows_pad, int max_col, int f_col,
+                                int *__restrict__ cols, double *__restrict__ vals) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows_pad; i += gridDim.x * blockDim.x) {
+    const int a = i < rows ? rp[i] : 0, len = i < rows ? rp[i + 1] - a : 0;
+    for (int s = 0; s < max_col; ++s) {
+      const size_t o = (size_t)s * rows_pad + i;
+      cols[o] = s < len ? ci[a + s] : (i < rows ? 0 : f_col);
+      vals[o] = s < len ? va[a + s] : 0.0;
+    }
+  }
+}
+
+// dense rows from sorted CSR arrays: runs of one column summed from 0 in order
+__global__ void dense_fill_kernel(const int *__restrict__ rp, const int *__restrict__ ci,
+                                  const double *__restrict__ va, int rows, int ld, double *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+    const int b = rp[i + 1];
+    for (int k = rp[i]; k < b;) {
+      const int c = ci[k];
+      double acc = 0.0;
+      for (; k < b && ci[k] == c; ++k) acc += va[k];
+      out[(size_t)i * ld + c] = acc;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace tbsla
+
+extern "C" tbsla_status_t tbsla_coo_to_ell(const tbsla_matrix_t *C, int stores, tbsla_matrix_t **out) {
+  TB_CHECK(C && out, "NULL argument");
+  *out = nullptr;
+  TB_CHECK(C->format == TBSLA_FMT_COO || C->format == TBSLA_FMT_SCOO, "tbsla_coo_to_ell needs a COO / SCOO handle");
+  tbsla_matrix_t *R = nullptr;
+  TB_TRY(tbsla_coo_to_csr(C, TBSLA_STORE_F64, &R));
+  struct Drop {
+    tbsla_matrix_t *R;
+    ~Drop() { free_matrix(R); }
+  } drop{R};
+  const int rows = R->rows;
+  std::vector<int> rp((size_t)rows + 1);
+  TB_CUDA(cudaMemcpy(rp.data(), R->idx0, rp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  int max_col = 0;
+  for (int i = 0; i < rows; ++i) max_col = std::max(max_col, rp[(size_t)i + 1] - rp[(size_t)i]);
+  tbsla_matrix *E = new_matrix(TBSLA_FMT_ELL);
+  if (!E) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  E->x_keep = 0.3f;
+  E->n_row = C->n_row; E->n_col = C->n_col; E->f_col = C->f_col;
+  E->rows = rows; E->max_col = max_col; E->rows_pad = (rows + 3) / 4 * 4;
+  const int64_t slots = (int64_t)rows * max_col, padded = (int64_t)E->rows_pad * max_col;
+  E->stored = slots;
+  E->x_extent = slots > 0 ? std::max<int64_t>(C->x_extent, 1) : 0;
+  double *vtmp = nullptr;
+  tbsla_status_t st = alloc_ints(E, &E->idx0, padded);
+  if (st == TBSLA_OK && cudaMalloc(&vtmp, (size_t)std::max<int64_t>(padded, 1) * 8) != cudaSuccess) {
+    cudaGetLastError();
+    st = fail(TBSLA_ERR_OOM, "conversion scratch");
+  }
+  if (st == TBSLA_OK && padded > 0) {
+    ell_fill_kernel<<<std::max(1, std::min((E->rows_pad + 255) / 256, 152 * 16)), 256>>>(
+        R->idx0, R->idx1, static_cast<const double *>(R->values[0]), rows, E->rows_pad, max_col, C->f_col, E->idx0,
+        vtmp);
+    if (cudaGetLastError() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "ELL fill kernel failed");
+  }
+  if (st == TBSLA_OK) st = store_values_device(E, vtmp, padded, stores, nullptr);
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "ELL conversion failed");
+  if (vtmp) cudaFree(vtmp);
+  if (st != TBSLA_OK) {
+    free_matrix(E);
+    return st;
+  }
+  *out = E;
+  return TBSLA_OK;
+}
+
+extern "C" tbsla_status_t tbsla_coo_to_dense(const tbsla_matrix_t *C, int stores, tbsla_matrix_t **out) {
+  TB_CHECK(C && out, "NULL argument");
+  *out = nullptr;
+  TB_CHECK(C->format == TBSLA_FMT_COO || C->format == TBSLA_FMT_SCOO,
+           "tbsla_coo_to_dense needs a COO / SCOO handle");
+  // the reference indexes the dense row with the stored column itself
+  TB_CHECK(C->stored == 0 || (int64_t)C->f_col + C->x_extent <= C->n_col,
+           "a stored column reaches past n_col = %d", C->n_col);
+  tbsla_matrix_t *R = nullptr;
+  TB_TRY(tbsla_coo_to_csr(C, TBSLA_STORE_F64, &R));
+  struct Drop {
+    tbsla_matrix_t *R;
+    ~Drop() { free_matrix(R); }
+  } drop{R};
+  tbsla_matrix *D = new_matrix(TBSLA_FMT_DENSE);
+  if (!D) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  const int ln_row = C->n_row, ln_col = C->n_col;
+  const int64_t n = (int64_t)ln_row * ln_col;
+  D->n_row = C->n_row; D->n_col = C->n_col; D->rows = ln_row; D->cols = ln_col;
+  D->stored = n;
+  D->x_extent = D->rows > 0 ? ln_col : 0;
+  double *vtmp = nullptr;
+  tbsla_status_t st = TBSLA_OK;
+  if (cudaMalloc(&vtmp, (size_t)std::max<int64_t>(n, 1) * 8) != cudaSuccess) {
+    cudaGetLastError();
+    st = fail(TBSLA_ERR_OOM, "dense conversion buffer (%lld doubles)", (long long)n);
+  }
+  if (st == TBSLA_OK && n > 0) {
+    cudaMemset(vtmp, 0, (size_t)n * 8);
+    if (R->stored > 0)
+      dense_fill_kernel<<<std::max(1, std::min((ln_row + 255) / 256, 152 * 16)), 256>>>(
+          R->idx0, R->idx1, static_cast<const double *>(R->values[0]), ln_row, ln_col, vtmp);
+    if (cudaGetLastError() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "dense fill kernel failed");
+  }
+  if (st == TBSLA_OK) st = store_values_device(D, vtmp, n, stores, nullptr);
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "dense conversion failed");
+  if (vtmp) cudaFree(vtmp);
+  if (st != TBSLA_OK) {
+    free_matrix(D);
+    return st;
+  }
+  *out = D;
+  return TBSLA_OK;
+}
+
+extern "C" tbsla_status_t tbsla_ell_download(const tbsla_matrix_t *A, int *columns, double *values) {
+  TB_CHECK(A && A->format == TBSLA_FMT_ELL, "not an ELL handle");
+  const int64_t padded = (int64_t)A->rows_pad * A->max_col;
+  if (padded == 0) return TBSLA_OK;
+  TB_CHECK(!values || A->values[0], "the F64 value store is not present");
+  std::vector<int> cm(columns ? (size_t)padded : 0);
+  std::vector<double> vm(values ? (size_t)padded : 0);
+  if (columns) TB_CUDA(cudaMemcpy(cm.data(), A->idx0, (size_t)padded * sizeof(int), cudaMemcpyDeviceToHost));
+  if (values) TB_CUDA(cudaMemcpy(vm.data(), A->values[0], (size_t)padded * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < A->rows; ++i)
+    for (int s = 0; s < A->max_col; ++s) {
+      const size_t o = (size_t)s * A->rows_pad + i, r = (size_t)i * A->max_col + s;
+      if (columns) columns[r] = cm[o];
+      if (values) values[r] = vm[o];
+    }
+  return TBSLA_OK;
+}
+
+extern "C" tbsla_status_t tbsla_dense_download(const tbsla_matrix_t *A, double *values) {
+  TB_CHECK(A && A->format == TBSLA_FMT_DENSE, "not a DENSE handle");
+  if (A->stored == 0 || !values) return TBSLA_OK;
+  TB_CHECK(A->values[0], "the F64 value store is not present");
+  TB_CUDA(cudaMemcpy(values, A->values[0], (size_t)A->stored * sizeof(double), cudaMemcpyDeviceToHost));
+  return TBSLA_OK;
+}
