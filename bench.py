@@ -204,13 +204,14 @@ def format_sweep(capi, peak, log2n=24):
     import torch
     out = {}
     n = 1 << log2n
+    nd = 32768 if log2n >= 24 else 8192  # DENSE order (small cases stay a few GB)
     cases = [("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
              ("CSR_bf16", "CSR", "cqmat", n, 16, 4, capi.BF16, capi.F32),
              ("ELL_f64", "ELL", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("COO_f64", "COO", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("SCOO_f64", "SCOO", "cqmat", n, 16, 1, capi.F64, capi.F64),
-             ("DENSE_f64_32768", "DENSE", "cqmat", 32768, 16, 1, capi.F64, capi.F64),
-             ("CSR_f64_cdiag_2^26", "CSR", "cdiag", 4 * n, 1, 1, capi.F64, capi.F64)]
+             (f"DENSE_f64_{nd}", "DENSE", "cqmat", nd, 16, 1, capi.F64, capi.F64),
+             (f"CSR_f64_cdiag_2^{log2n + 2}", "CSR", "cdiag", 4 * n, 1, 1, capi.F64, capi.F64)]
     for (key, fmt, gen, nn, c, stores, store, vt) in cases:
         A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
         i = A.info()
@@ -230,7 +231,7 @@ def format_sweep(capi, peak, log2n=24):
                     "stored": int(i.stored), "gflops": round(2 * i.stored / (ms * 1e-3) / 1e9, 1)}
         A.close()
         torch.cuda.empty_cache()
-    out["DENSE_multi_vector_32768_k64"] = dense_multi(capi, 32768 if log2n >= 24 else 8192, 64)
+    out[f"DENSE_multi_vector_{nd}_k64"] = dense_multi(capi, nd, 64)
     return out
 
 

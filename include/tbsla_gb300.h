@@ -380,6 +380,13 @@ tbsla_status_t tbsla_coo_to_ell(const tbsla_matrix_t *coo, int stores, tbsla_mat
  * column) pairs added to 0 in input order.  Stored columns must lie below
  * n_col (the reference indexes the dense row with them). */
 tbsla_status_t tbsla_coo_to_dense(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+/* COO handle -> SCOO handle: MatrixSCOO(const MatrixCOO&) (MatrixSCOO.cpp:
+ * 53-68) copies the arrays; here a device-to-device copy of the handle. */
+tbsla_status_t tbsla_coo_to_scoo(const tbsla_matrix_t *coo, int stores, tbsla_matrix_t **out);
+/* MatrixCSR::normalize_columns (MatrixCSR.cpp:423-435) on the device: each
+ * value divided by its column's sum, the sums accumulated in the reference's
+ * order (bit-identical values).  Derived stores and copies are refreshed. */
+tbsla_status_t tbsla_csr_normalize_columns(tbsla_matrix_t *A, void *stream);
 /* host copies in the reference's layouts: ELL columns / values row-major
  * (rows x max_col, MatrixELL::get_columns / get_values); DENSE values
  * (rows x ln_col).  Either pointer may be NULL. */

@@ -131,6 +131,8 @@ def lib() -> C.CDLL:
         "tbsla_coo_to_csr": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_ell": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_dense": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_coo_to_scoo": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_csr_normalize_columns": ([P, _vp], st),
         "tbsla_ell_download": ([P, _vp, _vp], st),
         "tbsla_dense_download": ([P, _vp], st),
         "tbsla_dense_spmm": ([P, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp], st),
@@ -425,6 +427,16 @@ class DeviceMatrix:
         h = _vp()
         check(lib().tbsla_coo_to_dense(self.h, stores, C.byref(h)))
         return DeviceMatrix(h)
+
+    def to_scoo(self, stores=STORE_F64):
+        """SCOO handle copied on the device from this COO / SCOO handle."""
+        h = _vp()
+        check(lib().tbsla_coo_to_scoo(self.h, stores, C.byref(h)))
+        return DeviceMatrix(h)
+
+    def normalize_columns(self, stream=None):
+        """MatrixCSR::normalize_columns on the device (CSR handles)."""
+        check(lib().tbsla_csr_normalize_columns(self.h, stream))
 
     def ell_download(self):
         """(columns, values) of an ELL handle, row-major rows x max_col."""

@@ -20,6 +20,7 @@ void free_matrix(tbsla_matrix *A);
 tbsla_status_t alloc_ints(tbsla_matrix *A, int **p, int64_t n);
 tbsla_status_t store_values_device(tbsla_matrix *A, const double *d_src, int64_t n, int stores, cudaStream_t s);
 tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp);
+tbsla_status_t alloc_carries(tbsla_matrix *A);
 
 namespace {
 
@@ -296,5 +297,46 @@ extern "C" tbsla_status_t tbsla_dense_download(const tbsla_matrix_t *A, double *
   if (A->stored == 0 || !values) return TBSLA_OK;
   TB_CHECK(A->values[0], "the F64 value store is not present");
   TB_CUDA(cudaMemcpy(values, A->values[0], (size_t)A->stored * sizeof(double), cudaMemcpyDeviceToHost));
+  return TBSLA_OK;
+}
+
+// MatrixSCOO(const MatrixCOO&) (src/cpp/matrix/MatrixSCOO.cpp:53-68) copies the
+// arrays and the block geometry: on the device, a copy of the handle's arrays
+// (device to device) under the SCOO tag, with its own row bins and carries.
+extern "C" tbsla_status_t tbsla_coo_to_scoo(const tbsla_matrix_t *C, int stores, tbsla_matrix_t **out) {
+  TB_CHECK(C && out, "NULL argument");
+  *out = nullptr;
+  TB_CHECK(C->format == TBSLA_FMT_COO || C->format == TBSLA_FMT_SCOO, "tbsla_coo_to_scoo needs a COO / SCOO handle");
+  TB_CHECK(C->values[0], "the conversion needs the F64 value store");
+  TB_CUDA(cudaSetDevice(C->device));
+  tbsla_matrix *S = new_matrix(TBSLA_FMT_SCOO);
+  if (!S) return fail(TBSLA_ERR_OOM, "host allocation failed");
+  const int64_t n = C->stored;
+  S->n_row = C->n_row; S->n_col = C->n_col; S->f_row = C->f_row; S->f_col = C->f_col;
+  S->rows = C->rows; S->stored = n; S->x_extent = C->x_extent; S->num_tiles = C->num_tiles;
+  S->csr_variant = C->csr_variant;
+  tbsla_status_t st = alloc_ints(S, &S->idx0, n);
+  if (st == TBSLA_OK) st = alloc_ints(S, &S->idx1, n);
+  if (st == TBSLA_OK && n > 0 &&
+      (cudaMemcpy(S->idx0, C->idx0, (size_t)n * 4, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+       cudaMemcpy(S->idx1, C->idx1, (size_t)n * 4, cudaMemcpyDeviceToDevice) != cudaSuccess))
+    st = fail(TBSLA_ERR_CUDA, "array copy failed");
+  if (st == TBSLA_OK) st = store_values_device(S, static_cast<const double *>(C->values[0]), n, stores, nullptr);
+  if (st == TBSLA_OK) st = alloc_carries(S);
+  if (st == TBSLA_OK && C->coo_rowptr && S->n_row > 0) {
+    std::vector<int> rp((size_t)S->n_row + 1);
+    st = alloc_ints(S, &S->coo_rowptr, (int64_t)S->n_row + 1);
+    if (st == TBSLA_OK &&
+        (cudaMemcpy(S->coo_rowptr, C->coo_rowptr, rp.size() * 4, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+         cudaMemcpy(rp.data(), C->coo_rowptr, rp.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess))
+      st = fail(TBSLA_ERR_CUDA, "row pointer copy failed");
+    if (st == TBSLA_OK) st = csr_bins(S, rp);
+  }
+  if (st == TBSLA_OK && cudaDeviceSynchronize() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "SCOO copy failed");
+  if (st != TBSLA_OK) {
+    free_matrix(S);
+    return st;
+  }
+  *out = S;
   return TBSLA_OK;
 }

@@ -197,7 +197,7 @@ tbsla_status_t store_values_device(tbsla_matrix *A, const double *d_src, int64_t
 tbsla_matrix *new_matrix(int format);
 void free_matrix(tbsla_matrix *A);
 
-static tbsla_status_t alloc_carries(tbsla_matrix *A) {
+tbsla_status_t alloc_carries(tbsla_matrix *A) {
   const int nt = std::max(A->num_tiles, 1);
   TB_TRY(alloc_n(A, &A->tile_head_row, nt));
   TB_TRY(alloc_n(A, &A->tile_head_val, nt));

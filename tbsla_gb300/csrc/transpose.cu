@@ -215,3 +215,61 @@ tbsla_status_t tbsla_csr_grad_values(const tbsla_matrix_t *A, tbsla_dtype_t type
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- normalize_columns
+// MatrixCSR::normalize_columns (src/cpp/matrix/MatrixCSR.cpp:423-435) on the
+// device: column sums accumulated from 0 in the order of the reference's
+// loop (rows ascending, then stored order) -- the transposed copy lists each
+// column's entries in exactly that order, so one thread per column repeats
+// the reference's additions -- then every value divided by its column's sum
+// (IEEE division, as the host's).  The values then go through
+// tbsla_matrix_set_values, which refreshes every derived copy.
+namespace tbsla {
+namespace {
+
+__global__ void colsum_kernel(const int *__restrict__ tp, const double *__restrict__ tv, int ncol,
+                              double *__restrict__ sum) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ncol; j += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = tp[j]; k < tp[j + 1]; ++k) s += tv[k];
+    sum[j] = s;
+  }
+}
+
+__global__ void divide_kernel(const double *__restrict__ v, const int *__restrict__ ci, int f_col, int64_t n,
+                              const double *__restrict__ sum, double *__restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = v[k] / sum[ci[k] - f_col];
+}
+
+}  // namespace
+}  // namespace tbsla
+
+extern "C" tbsla_status_t tbsla_csr_normalize_columns(tbsla_matrix_t *A, void *stream) {
+  TB_CHECK(A, "matrix is NULL");
+  TB_CHECK(A->format == TBSLA_FMT_CSR, "tbsla_csr_normalize_columns needs a CSR handle");
+  TB_CHECK(A->values[0], "the F64 value store is needed");
+  TB_CUDA(cudaSetDevice(A->device));
+  if (A->stored == 0) return TBSLA_OK;
+  tbsla_matrix *T = nullptr;
+  TB_TRY(ensure_transpose(A, &T));
+  cudaStream_t s = (cudaStream_t)stream;
+  double *sum = nullptr, *out = nullptr;
+  const int ncol = std::max(A->n_col, 1);
+  if (cudaMalloc(&sum, (size_t)ncol * 8) != cudaSuccess || cudaMalloc(&out, (size_t)A->stored * 8) != cudaSuccess) {
+    cudaGetLastError();
+    if (sum) cudaFree(sum);
+    return fail(TBSLA_ERR_OOM, "normalize_columns scratch");
+  }
+  tbsla_status_t st = TBSLA_OK;
+  colsum_kernel<<<std::max(1, std::min((T->rows + 255) / 256, 152 * 16)), 256, 0, s>>>(
+      T->idx0, static_cast<const double *>(T->values[0]), T->rows, sum);
+  divide_kernel<<<152 * 8, 256, 0, s>>>(static_cast<const double *>(A->values[0]), A->idx1, A->f_col, A->stored, sum,
+                                       out);
+  if (cudaGetLastError() != cudaSuccess) st = fail(TBSLA_ERR_CUDA, "normalize_columns kernels failed");
+  if (st == TBSLA_OK) st = tbsla_matrix_set_values(A, TBSLA_F64, out, stream);
+  cudaStreamSynchronize(s);
+  cudaFree(sum);
+  cudaFree(out);
+  return st;
+}

@@ -74,3 +74,48 @@ def test_coo_to_ell_and_dense(gpu, orc):
         if nnz > 10:
             val[-1] = -0.0
         _check_ell_dense(gpu, orc, nr, nc, row, col, val)
+
+
+def test_coo_to_scoo_copy(gpu, orc):
+    """MatrixSCOO(COO) copies the arrays: the device copy gives the same
+    products (every kernel variant, row shifts) as the COO handle."""
+    rng = np.random.default_rng(5)
+    n_row, n_col, nnz = 3000, 2000, 40000
+    row = rng.integers(0, n_row, nnz).astype(np.int32)
+    col = rng.integers(0, n_col, nnz).astype(np.int32)
+    val = rng.standard_normal(nnz)
+    C = gpu.DeviceMatrix.coo(n_row, n_col, row, col, val)
+    S = C.to_scoo(stores=gpu.STORE_F64 | gpu.STORE_F32)
+    i, j = C.info(), S.info()
+    assert (i.n_row, i.n_col, i.stored) == (j.n_row, j.n_col, j.stored)
+    x = rng.uniform(-1, 1, n_col)
+    for v in (0, 1):
+        C.set_variant(v)
+        S.set_variant(v)
+        for incr in (0, 2):
+            assert np.array_equal(C.spmv_host(x, incr), S.spmv_host(x, incr)), f"variant {v} shift {incr}"
+
+
+def test_csr_normalize_columns(gpu, orc):
+    """MatrixCSR::normalize_columns on the device: values bit-identical to the
+    oracle's restatement (column sums in the reference's loop order), the
+    derived FP32 store and the transposed copy refreshed."""
+    rng = np.random.default_rng(6)
+    for (nr, nc, nnz) in [(1, 1, 1), (500, 300, 4000), (20000, 15000, 300000)]:
+        row = np.sort(rng.integers(0, nr, nnz)).astype(np.int64)
+        rp = np.zeros(nr + 1, np.int64)
+        np.add.at(rp, row + 1, 1)
+        rp = np.cumsum(rp).astype(np.int32)
+        ci = rng.integers(0, nc, nnz).astype(np.int32)
+        va = rng.uniform(0.1, 2.0, nnz)
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32)
+        m.spmv_host(rng.uniform(-1, 1, nc))
+        m.normalize_columns()
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        o.normalize_columns()
+        ov = o.arrays.values
+        _, _, got = m.csr_download()
+        assert np.array_equal(got.view(np.int64), ov.view(np.int64))
+        B = gpu.DeviceMatrix.csr(nr, nc, rp, ci, ov)
+        xc = rng.uniform(-1, 1, nc)
+        assert np.array_equal(m.spmv_host(xc), B.spmv_host(xc))
