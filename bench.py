@@ -4,8 +4,9 @@ Headline (``value``): CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24, c = 16
 q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of algorithmic traffic per
 product), in GB/s of algorithmic bytes over device time with the matrix and x
 resident in HBM.  A "step" is one product.  ``e2e`` is the same metric through
-the C ABI's host-vector call (tbsla_spmv_host): pinned x copied in, y copied
-out, both inside the timed region.
+the C ABI's host-vector call (tbsla_spmv_host) on pinned host vectors: x is
+copied into HBM and the product writes y into host memory over NVLink-C2C,
+both inside the timed region.
 
 Also reported (single-GPU runs): the format sweep of the same configuration
 (ELL/COO/SCOO FP64, CSR FP32/BF16 stores, DENSE n = 32768, cdiag n = 2^26) and

@@ -789,6 +789,103 @@ tbsla_status_t tbsla_spmv_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   return spmv_dispatch(A, store, x_type, d_x, y_type, d_y, vect_incr, (cudaStream_t)stream);
 }
 
+}  // extern "C"
+
+namespace tbsla {
+namespace {
+
+// whether the device reads and writes pageable host memory coherently (the
+// NVLink-C2C / address-translation path of Grace-Blackwell), per device
+bool pageable_access(int dev) {
+  static int cache[64];
+  static std::once_flag once[64];
+  if (dev < 0 || dev >= 64) return false;
+  std::call_once(once[dev], [dev] {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    cache[dev] = v;
+  });
+  return cache[dev] != 0;
+}
+
+// The pointer a kernel uses for host memory p: the device alias of pinned
+// memory, p itself for pageable memory the device reaches coherently,
+// nullptr otherwise (or for memory that is not host memory).
+void *device_alias(void *p, int dev) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  if (a.type == cudaMemoryTypeUnregistered && pageable_access(dev)) return p;
+  return nullptr;
+}
+
+// host -> device copy of n doubles by the SMs, for pageable sources the
+// device reads coherently (the copy engines would stage them through a
+// pinned bounce buffer)
+__global__ void __launch_bounds__(256) host_read2_kernel(const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                                        int64_t n2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+__global__ void __launch_bounds__(256) host_read1_kernel(const double *__restrict__ src, double *__restrict__ dst,
+                                                        int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+tbsla_status_t stage_x(tbsla_matrix *A, const double *x, int64_t nx) {
+  if (!nx) return TBSLA_OK;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, x) != cudaSuccess) {
+    cudaGetLastError();
+    a.type = cudaMemoryTypeUnregistered;
+  }
+  if (a.type == cudaMemoryTypeUnregistered && pageable_access(A->device)) {
+    const int grid = 152 * 4;
+    if ((reinterpret_cast<uintptr_t>(x) & 15) == 0) {
+      host_read2_kernel<<<grid, 256, 0, A->stream>>>(reinterpret_cast<const double2 *>(x),
+                                                     reinterpret_cast<double2 *>(A->d_x), nx / 2);
+      if (nx & 1) host_read1_kernel<<<1, 32, 0, A->stream>>>(x + nx - 1, A->d_x + nx - 1, 1);
+    } else {
+      host_read1_kernel<<<grid, 256, 0, A->stream>>>(x, A->d_x, nx);
+    }
+    TB_CUDA(cudaGetLastError());
+    return TBSLA_OK;
+  }
+  TB_CUDA(cudaMemcpyAsync(A->d_x, x, nx * sizeof(double), cudaMemcpyHostToDevice, A->stream));
+  return TBSLA_OK;
+}
+
+}  // namespace
+
+// whether the product writes every row of y itself (zero_unwritten would
+// leave y alone), so y may be written in place wherever it lives
+bool writes_all_rows(const tbsla_matrix *A, int vect_incr) {
+  if (A->n_row <= 0) return false;
+  if (A->format == TBSLA_FMT_COO || A->format == TBSLA_FMT_SCOO)
+    return A->coo_rowptr && A->csr_variant == 0 && vect_incr == 0 && A->stored > 0;
+  if (A->format == TBSLA_FMT_ELL && A->max_col == 0) return false;
+  if (A->format == TBSLA_FMT_DENSE && A->cols == 0) return false;
+  if (A->format == TBSLA_FMT_CSR && A->stored == 0) return false;
+  return A->rows >= A->n_row;
+}
+
+}  // namespace tbsla
+
+extern "C" {
+
+// Host vectors: x is staged into the handle's device buffer (a copy-engine
+// copy from pinned memory, an SM copy from pageable memory the device reads
+// coherently); when the product writes every row, y is written in place in
+// host memory by the product itself (pinned or coherent pageable memory),
+// so no device-to-host copy follows and y's traffic leaves HBM to the matrix.
 tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *y,
                                int64_t ny, int vect_incr) {
   TB_CHECK(A, "matrix is NULL");
@@ -797,10 +894,12 @@ tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, d
   TB_CHECK(nx == 0 || x, "x is NULL");
   std::lock_guard<std::mutex> lk(A->host_mu);
   TB_CUDA(cudaSetDevice(A->device));
-  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), std::max<int64_t>(ny, 1), 0));
-  if (nx) TB_CUDA(cudaMemcpyAsync(A->d_x, x, nx * sizeof(double), cudaMemcpyHostToDevice, A->stream));
-  TB_TRY(spmv_dispatch(A, TBSLA_F64, TBSLA_F64, A->d_x, TBSLA_F64, A->d_y, vect_incr, A->stream));
-  if (A->n_row) TB_CUDA(cudaMemcpyAsync(y, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
+  double *y_dev = writes_all_rows(A, vect_incr) ? static_cast<double *>(device_alias(y, A->device)) : nullptr;
+  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), y_dev ? 1 : std::max<int64_t>(ny, 1), 0));
+  TB_TRY(stage_x(A, x, nx));
+  TB_TRY(spmv_dispatch(A, TBSLA_F64, TBSLA_F64, A->d_x, TBSLA_F64, y_dev ? y_dev : A->d_y, vect_incr, A->stream));
+  if (!y_dev && A->n_row)
+    TB_CUDA(cudaMemcpyAsync(y, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
   TB_CUDA(cudaStreamSynchronize(A->stream));
   return TBSLA_OK;
 }
@@ -820,10 +919,13 @@ tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx,
   TB_CHECK(nx >= A->n_col && nr >= A->n_row && nx >= A->x_extent, "vector too short");
   std::lock_guard<std::mutex> lk(A->host_mu);
   TB_CUDA(cudaSetDevice(A->device));
-  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), std::max<int64_t>(nr, 1), std::max(A->n_row, 1)));
-  if (nx) TB_CUDA(cudaMemcpyAsync(A->d_x, x, nx * sizeof(double), cudaMemcpyHostToDevice, A->stream));
-  TB_TRY(a_axpx_dispatch(A, A->d_x, A->d_y, A->d_t, vect_incr, A->stream));
-  if (A->n_row) TB_CUDA(cudaMemcpyAsync(r, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
+  // r is written in place by the second product when it writes every row
+  double *r_dev = writes_all_rows(A, vect_incr) ? static_cast<double *>(device_alias(r, A->device)) : nullptr;
+  TB_TRY(ensure_host_buffers(A, std::max<int64_t>(nx, 1), r_dev ? 1 : std::max<int64_t>(nr, 1), std::max(A->n_row, 1)));
+  TB_TRY(stage_x(A, x, nx));
+  TB_TRY(a_axpx_dispatch(A, A->d_x, r_dev ? r_dev : A->d_y, A->d_t, vect_incr, A->stream));
+  if (!r_dev && A->n_row)
+    TB_CUDA(cudaMemcpyAsync(r, A->d_y, (size_t)A->n_row * sizeof(double), cudaMemcpyDeviceToHost, A->stream));
   TB_CUDA(cudaStreamSynchronize(A->stream));
   return TBSLA_OK;
 }
