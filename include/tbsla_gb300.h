@@ -347,7 +347,7 @@ tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pager
  * nodes[offsets[c] .. offsets[c+1]) (repeated seeds count once), and stops on
  * its own when its L1 change is below p->tol or after p->max_iter sweeps;
  * stopped vectors are frozen while the others continue.  The iterates are
- * multiplied in tiles of `tile` vectors (8, 16 or 32; 0 picks one) as one
+ * multiplied in tiles of `tile` vectors (2, 4, 8, 16 or 32; 0 picks one) as one
  * multi-vector product per tile.  p->precision: TBSLA_F64, or TBSLA_F32
  * (F32 value store and FP32 iterates).  d_out: n*k doubles, vector c at
  * d_out + c*n; iterations / residuals: k host entries each, or NULL.

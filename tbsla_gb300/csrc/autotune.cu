@@ -154,7 +154,9 @@ tbsla_status_t tbsla_autotune_ppr(tbsla_matrix_t *A, int k, tbsla_dtype_t precis
   p.mode = TBSLA_PR_TELEPORT;
   p.precision = precision;
   p.check_every = 3;
-  const int tiles[] = {8, 16, 32};
+  // narrow tiles keep a tile's iterates in L2 (n * KT values), wide ones
+  // stream the matrix fewer times per vector
+  const int tiles[] = {2, 4, 8, 16, 32};
   float best = 1e30f;
   int best_t = 32, tried = 0;
   tbsla_status_t st = TBSLA_OK;
