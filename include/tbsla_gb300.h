@@ -169,8 +169,12 @@ tbsla_status_t tbsla_spmv_ex(const tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
                              void *stream);
 
 /* Synchronous host-vector form used by the drop-in classes
- * (std::vector<double> in, std::vector<double> out): copies x (nx entries)
- * to the device, runs tbsla_spmv, copies y (ny >= n_row entries) back. */
+ * (std::vector<double> in, std::vector<double> out): x (nx entries) goes to
+ * the device (copy engine from pinned memory, an SM copy from pageable
+ * memory the device reads coherently), then tbsla_spmv.  When the product
+ * writes every row and y (ny >= n_row entries) is pinned or coherently
+ * reachable pageable memory, the product writes y in place over NVLink-C2C;
+ * otherwise y is copied back. */
 tbsla_status_t tbsla_spmv_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *y,
                                int64_t ny, int vect_incr);
 
@@ -206,8 +210,8 @@ tbsla_status_t tbsla_dense_spmm(const tbsla_matrix_t *A, tbsla_dtype_t store, in
                                 int64_t ldx, void *d_Y, int64_t ldy, void *stream);
 
 /* r = A (A x + x): Matrix::a_axpx_ (Matrix.cpp:6-11), square matrices; the
- * "+ x" is fused into the first product.  d_tmp: n_row doubles of scratch or
- * NULL to use the handle's own. */
+ * "+ x" is fused into the first product.  d_tmp: n_row doubles of device
+ * scratch (required: the call is stream-ordered and holds no handle lock). */
 tbsla_status_t tbsla_a_axpx(const tbsla_matrix_t *A, const double *d_x, double *d_r,
                             double *d_tmp, int vect_incr, void *stream);
 tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx, double *r,

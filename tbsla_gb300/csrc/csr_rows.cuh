@@ -1,4 +1,5 @@
-// csr_rows.cuh -- row-block CSR SpMV for sm_103a (the default CSR kernel).
+// csr_rows.cuh -- row-block CSR SpMV for sm_103a (kernel variant 1 of CSR handles,
+// tbsla_matrix_set_variant; the direct kernels of csr_direct.cuh are the default).
 //
 // The matrix is cut at creation into blocks of whole rows holding at most
 // kRowsMax rows, kRowsMax segments (a segment: at most kSeg consecutive
