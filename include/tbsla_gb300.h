@@ -77,6 +77,16 @@ const char *tbsla_status_string(tbsla_status_t s);
 int tbsla_version(void);
 /* device the library uses for new handles (default: current device) */
 tbsla_status_t tbsla_set_device(int device);
+/* The current device's L2 fetch granularity for this process (the CUDA
+ * context limit cudaLimitMaxL2FetchGranularity; 32, 64 or 128 bytes): how
+ * much a missing load brings from DRAM.  The short-row CSR kernel asks for
+ * 256-byte prefetches on its streamed row data, so at 32 bytes the random
+ * gathers of x stop bringing unused sectors while the streams stay wide
+ * (cqmat 2^24 FP64: 4396 GB/s at 32 against 4283 at the context's default).
+ * Kernels that stream without such hints (the long-row and ELL kernels) lose
+ * at 32; the setting is the caller's, process-wide, and ends with it. */
+tbsla_status_t tbsla_set_l2_fetch_granularity(int bytes);
+tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes);
 
 /* ------------------------------------------------------------ matrices */
 /* CSR from host arrays.  Replaces MatrixCSR(n_row, n_col, values, rowptr,

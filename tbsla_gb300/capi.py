@@ -132,6 +132,8 @@ def lib() -> C.CDLL:
         "tbsla_coo_to_ell": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_dense": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_coo_to_scoo": ([P, C.c_int, C.POINTER(P)], st),
+        "tbsla_set_l2_fetch_granularity": ([C.c_int], st),
+        "tbsla_get_l2_fetch_granularity": ([C.POINTER(C.c_int)], st),
         "tbsla_csr_normalize_columns": ([P, _vp], st),
         "tbsla_ell_download": ([P, _vp, _vp], st),
         "tbsla_dense_download": ([P, _vp], st),

@@ -44,33 +44,31 @@ __device__ __forceinline__ float bf16_hi(unsigned w) { return __bfloat162float(_
 // eight entries from an 8-aligned index with 16-byte loads through L1 and the
 // default cache policy (arrays carry 64 bytes of padding, so a group may run
 // past the last entry).  A lane reads each sector in two pieces; L1/L2 keep
-// the line between them.  Explicit L2 hints were measured worse here: an
-// evict-first hint lets L2 drop the line between the two reads (DRAM traffic
-// x2.5), and 32-byte loads with an evict-normal policy ran 20% slower.
+// the line between them.  Explicit L2 eviction hints were measured worse
+// here: an evict-first hint lets L2 drop the line between the two reads
+// (DRAM traffic x2.5), and 32-byte loads with an evict-normal policy ran 20%
+// slower.  FP64 values and the column indices ask for 256-byte L2 prefetches:
+// neutral at the default L2 fetch granularity, and they keep the streams
+// wide when the process lowers it to 32 bytes for the gathers
+// (tbsla_set_l2_fetch_granularity).
 __device__ __forceinline__ void ld_vals8(const double *p, double (&v)[8]) {
   #pragma unroll
-  for (int h = 0; h < 4; ++h) {
-    const double2 d = __ldg(reinterpret_cast<const double2 *>(p) + h);
-    v[2 * h] = d.x; v[2 * h + 1] = d.y;
-  }
+  for (int h = 0; h < 4; ++h)
+    asm("ld.global.nc.L2::256B.v2.f64 {%0,%1}, [%2];" : "=d"(v[2 * h]), "=d"(v[2 * h + 1]) : "l"(p + 2 * h));
 }
 __device__ __forceinline__ void ld_vals8(const float *p, float (&v)[8]) {
-  const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
-  const float4 b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  asm("ld.global.nc.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "l"(p));
+  asm("ld.global.nc.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]) : "l"(p + 4));
 }
 __device__ __forceinline__ void ld_vals8(const __nv_bfloat16 *p, float (&v)[8]) {
-  const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
-  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+  unsigned w[4];
+  asm("ld.global.nc.L2::256B.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]) : "l"(p));
   #pragma unroll
   for (int h = 0; h < 4; ++h) { v[2 * h] = bf16_lo(w[h]); v[2 * h + 1] = bf16_hi(w[h]); }
 }
 __device__ __forceinline__ void ld_cols8(const int *c, int (&col)[8]) {
-  const int4 a = __ldg(reinterpret_cast<const int4 *>(c));
-  const int4 b = __ldg(reinterpret_cast<const int4 *>(c) + 1);
-  col[0] = a.x; col[1] = a.y; col[2] = a.z; col[3] = a.w;
-  col[4] = b.x; col[5] = b.y; col[6] = b.z; col[7] = b.w;
+  asm("ld.global.nc.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4];" : "=r"(col[0]), "=r"(col[1]), "=r"(col[2]), "=r"(col[3]) : "l"(c));
+  asm("ld.global.nc.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4];" : "=r"(col[4]), "=r"(col[5]), "=r"(col[6]), "=r"(col[7]) : "l"(c + 4));
 }
 // two entries from an even index
 __device__ __forceinline__ void ld_vals2(const double *p, double (&v)[2]) {
@@ -248,22 +246,22 @@ constexpr int kStageCapMax = 32 * kShortRow;  // a tile's entries when every row
 template <typename T> __device__ __forceinline__ T ld_first(const T *p, uint64_t pol);
 template <> __device__ __forceinline__ double ld_first<double>(const double *p, uint64_t pol) {
   double v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
   return v;
 }
 template <> __device__ __forceinline__ float ld_first<float>(const float *p, uint64_t pol) {
   float v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
   return v;
 }
 template <> __device__ __forceinline__ int ld_first<int>(const int *p, uint64_t pol) {
   int v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
   return v;
 }
 template <> __device__ __forceinline__ __nv_bfloat16 ld_first<__nv_bfloat16>(const __nv_bfloat16 *p, uint64_t pol) {
   unsigned short v;
-  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.L2::256B.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(pol));
   return __ushort_as_bfloat16(v);
 }
 

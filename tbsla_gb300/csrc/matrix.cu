@@ -508,6 +508,22 @@ const char *tbsla_status_string(tbsla_status_t s) {
 
 int tbsla_version(void) { return 100; }
 
+tbsla_status_t tbsla_set_l2_fetch_granularity(int bytes) {
+  TB_CHECK(bytes == 32 || bytes == 64 || bytes == 128, "L2 fetch granularity %d not 32, 64 or 128", bytes);
+  TB_CUDA(cudaSetDevice(current_device()));
+  TB_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes) {
+  TB_CHECK(bytes, "bytes is NULL");
+  TB_CUDA(cudaSetDevice(current_device()));
+  size_t v = 0;
+  TB_CUDA(cudaDeviceGetLimit(&v, cudaLimitMaxL2FetchGranularity));
+  *bytes = (int)v;
+  return TBSLA_OK;
+}
+
 tbsla_status_t tbsla_set_device(int device) {
   int n = 0;
   TB_CUDA(cudaGetDeviceCount(&n));

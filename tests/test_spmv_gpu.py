@@ -365,3 +365,21 @@ def test_csr_staged_kernel(gpu, orc):
     # the per-block partial sums group rows differently: equal to rounding
     assert abs(r0.iterations - r1.iterations) <= 1 and r1.converged
     assert float(np.abs(x0 - x1).sum()) <= 1e-11
+
+
+def test_l2_fetch_granularity(gpu):
+    """The process-wide L2 fetch granularity is set and read back; products
+    do not depend on it (32-byte fetches with 256-byte prefetched rows)."""
+    L = gpu.lib()
+    v = C.c_int()
+    g = gpu.generate("CSR", "cqmat", 30000, 30000, 16, 0.1, 0)
+    m = gpu.DeviceMatrix.from_generated(g)
+    x = np.random.default_rng(4).uniform(-1, 1, 30000)
+    ys = []
+    for b in (32, 64, 128):
+        gpu.check(L.tbsla_set_l2_fetch_granularity(b))
+        gpu.check(L.tbsla_get_l2_fetch_granularity(C.byref(v)))
+        assert v.value == b
+        ys.append(m.spmv_host(x))
+    assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[0], ys[2])
+    assert L.tbsla_set_l2_fetch_granularity(48) != 0
