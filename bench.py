@@ -46,10 +46,10 @@ Q_HEADLINE = 0.1
 L2_FETCH_HEADLINE = 32  # bytes (tbsla_set_l2_fetch_granularity)
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
-# DRAM bytes (read + write) of one csr_short_kernel launch on the 2^24
+# DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
 # workload, from the ncu capture summarised in
-# profiles/csr_short_kernel_cqmat_2p24.md
-NCU_TRAFFIC_BYTES = 4_214_376_448
+# profiles/csr_pair_kernel_cqmat_2p24.md
+NCU_TRAFFIC_BYTES = 4_128_661_388
 
 
 def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):
@@ -586,7 +586,7 @@ def run_gb300(args, world, rank, local, pg):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": NCU_TRAFFIC_BYTES if args.log2n == 24 else None,
-                     "kernel": "csr_short_kernel", "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "csr_pair_kernel", "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel_ms": round(kern_avg_ms, 4)},
         "cpu_baseline": {"value": round(cpu_gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": "full matrix, median of 5 products (oracle CSR loop, OpenMP over rows)"},

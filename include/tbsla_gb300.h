@@ -141,11 +141,17 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         address (the same lines on every load: an L2
  *                         range policy); 0 (default): a fraction of the
  *                         lines touched.
- *   TBSLA_TUNE_CSR_STAGE  1: when every row holds at most 32 entries, the
- *                         CSR product stages each 32-row tile's entries in
- *                         shared memory with coalesced loads and sums each
- *                         row from there (one thread per row); 0: rows are
- *                         read straight from global memory.
+ *   TBSLA_TUNE_SHORT_ROWS the kernel for rows of at most 32 entries:
+ *                         -1 (default) 2 for plain products of FP64 values
+ *                         when the short rows average 8 entries or more, 0
+ *                         otherwise (PageRank sweeps, FP32 / BF16 stores);
+ *                         0 one thread per row, summed in stored
+ *                         order; 1 (every row short) each 32-row tile's
+ *                         entries staged in shared memory with coalesced
+ *                         loads, rows summed from there in stored order
+ *                         (bit-identical to 0); 2 two lanes per row, each
+ *                         summing half the row in stored order, row = first
+ *                         half + second half (rounds differently from 0).
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)
@@ -157,7 +163,7 @@ typedef enum {
   TBSLA_TUNE_X_L2_KEEP = 0,
   TBSLA_TUNE_PR_RELABEL = 1,
   TBSLA_TUNE_X_L2_RANGE = 2,
-  TBSLA_TUNE_CSR_STAGE = 3
+  TBSLA_TUNE_SHORT_ROWS = 3
 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
@@ -276,11 +282,12 @@ tbsla_status_t tbsla_batch_destroy(tbsla_batch_t *B);
 typedef struct {
   int candidates;   /* candidates timed                         */
   float best_ms;    /* time of the kept one                     */
-  int choice;       /* spmv: 0 direct, 1 row blocks, 2 staged short rows;
+  int choice;       /* spmv: 0 direct, 1 row blocks, 2 staged short rows,
+                       3 two lanes per short row;
                        batch: blocks per SM; ppr: tile */
   double value;     /* spmv: x L2-keep fraction; otherwise = choice */
 } tbsla_autotune_result_t;
-/* CSR kernel variant, TBSLA_TUNE_CSR_STAGE and TBSLA_TUNE_X_L2_KEEP for the
+/* CSR kernel variant, TBSLA_TUNE_SHORT_ROWS and TBSLA_TUNE_X_L2_KEEP for the
  * `store` product (COO / SCOO: the staged kernel and the keep fraction) */
 tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla_autotune_result_t *res);
 /* persistent grid of a bound batch */

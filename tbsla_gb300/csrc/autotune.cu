@@ -4,7 +4,7 @@
 // (after one untimed run of each, so first-touch costs do not count), keeps
 // the fastest, and stores it where the library reads it: the CSR product's
 // kernel variant, staged short-row kernel and x L2-keep fraction
-// (tbsla_matrix_set_variant / TBSLA_TUNE_CSR_STAGE / TBSLA_TUNE_X_L2_KEEP),
+// (tbsla_matrix_set_variant / TBSLA_TUNE_SHORT_ROWS / TBSLA_TUNE_X_L2_KEEP),
 // the persistent grid of a matrix batch
 // (tbsla_batch_tune), the tile width of batched PageRank (used when
 // tbsla_ppr_batched is called with tile 0).  Results never depend on these
@@ -67,19 +67,22 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
   const float keeps[] = {0.0f, 0.3f, 0.6f, 1.0f};
   // kernels: 0 direct, 1 row blocks (CSR), 2 direct with the staged
-  // short-row kernel (every row at most 32 entries)
+  // short-row kernel (every row at most 32 entries), 3 direct with two lanes
+  // per short row
   const bool csr = A->format == TBSLA_FMT_CSR;
   float best = 1e30f;
-  int best_v = A->csr_variant == 0 && A->stage_mode > 0 ? 2 : A->csr_variant;
+  int best_v = A->csr_variant == 1 ? 1 : A->short_mode == 1 ? 2 : A->short_mode == 2 ? 3 : 0;
+  const int mode_in = A->short_mode;
   float best_k = A->x_keep;
   tbsla_status_t st = TBSLA_OK;
   int tried = 0;
-  for (int v = 0; v < 3 && st == TBSLA_OK; ++v) {
+  for (int v = 0; v < 4 && st == TBSLA_OK; ++v) {
     if (v == 1 && !csr) continue;
     if (v == 2 && A->stage_cap == 0) continue;
+    if (v == 3 && A->n_short == 0) continue;
     for (float k : keeps) {
       if (csr) A->csr_variant = v == 1 ? 1 : 0;
-      A->stage_mode = v == 2 ? 1 : 0;
+      A->short_mode = v == 2 ? 1 : v == 3 ? 2 : 0;
       A->x_keep = k;
       float ms = 0;
       st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
@@ -94,8 +97,9 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   cudaFree(x);
   cudaFree(y);
   if (csr) A->csr_variant = best_v == 1 ? 1 : 0;
-  A->stage_mode = best_v == 2 ? 1 : 0;
-  if (A->pr_relabel) A->pr_relabel->stage_mode = A->stage_mode;
+  A->short_mode = best_v == 2 ? 1 : best_v == 3 ? 2 : 0;
+  if (tried == 0) A->short_mode = mode_in;
+  if (A->pr_relabel) A->pr_relabel->short_mode = A->short_mode;
   A->x_keep = best_k;
   if (res) {
     res->candidates = tried;

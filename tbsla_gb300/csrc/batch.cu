@@ -6,7 +6,8 @@
 // static stride (block b takes items b, b + grid, ...), so the order of every
 // sum is fixed and the launch needs no counter to reset: it can be replayed
 // from a CUDA graph as is.  A row is summed by one thread in its stored
-// order (the thread-per-row loads of csr_direct.cuh).  An optional device
+// order (the thread-per-row loads of csr_direct.cuh: the single products'
+// arithmetic with TBSLA_TUNE_SHORT_ROWS = 0).  An optional device
 // mask skips members (per-instance convergence masking for iterative
 // callers).
 #include <algorithm>

@@ -90,10 +90,15 @@ struct tbsla_matrix {
   // items (long rows and chunks of huge rows), huge rows, chunk partials
   int *short_rows = nullptr;
   int n_short = 0;
+  int64_t short_nnz = 0;  // entries of the short rows
   // all rows short: shared-memory slots per warp of the staged kernel (the
   // entries of the largest 32-row tile, a multiple of 16); 0 otherwise
   int stage_cap = 0;
-  int stage_mode = 0;  // staged kernel: 1 on, 0 off (tbsla_matrix_tune)
+  // short-row kernel (tbsla_matrix_tune): 0 one thread per row, 1 staged
+  // tiles (every row short), 2 two lanes per row, -1 (default) two lanes for
+  // plain products of FP64 values when short rows average at least
+  // kPairMinRow entries, one thread per row otherwise
+  int short_mode = -1;
   int4 *warp_items = nullptr;
   int n_warp_items = 0;
   int item_class_start[5] = {0, 0, 0, 0, 0};  // items of length class c: [start[c], start[c+1])

@@ -1,7 +1,9 @@
 // csr_direct.cuh -- direct CSR SpMV kernels for sm_103a (the default CSR path).
 //
 // Rows are binned at creation by length:
-//   short (<= kShortRow nonzeros): one thread per row, walking its row in
+//   short (<= kShortRow nonzeros), plain FP64 products of rows averaging at
+//     least kPairMinRow entries: two lanes per row (csr_pair_kernel, below).
+//   short, otherwise: one thread per row, walking its row in
 //     chunks of eight entries with 16-byte loads straight from global memory.
 //     Lanes of a warp hold neighbouring rows; the loads of one chunk are
 //     issued together, so a sector's second use hits the line already in
@@ -172,6 +174,53 @@ __global__ void __launch_bounds__(256) csr_short_kernel(const int *__restrict__ 
       a = an;
       b = bn;
     }
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
+// Short rows, two adjacent lanes per row: the row's aligned groups (of eight
+// entries, or of two for rows under eight) are split in halves, each lane
+// sums its half in stored order, and the row is first half + second half (a
+// fixed order: results do not depend on scheduling, but round differently
+// from the one-lane sum).  A warp's load instruction touches 16 rows' lines
+// instead of 32, for one more FP64 add per row.
+// the default uses the pairs for FP64 plain products when short rows
+// average at least this many entries (cqmat c=16: 4889 vs 4378 GB/s with
+// 32-byte L2 fetches; cdiag, 2 per row: 2516 vs 4647 -- a lane idles)
+constexpr int kPairMinRow = 8;
+
+template <typename V, typename XT, typename Acc>
+__device__ __forceinline__ Acc row_half(const int *__restrict__ colidx, const V *__restrict__ values,
+                                        const XT *__restrict__ x, int f_col, int a, int b, int half,
+                                        uint64_t keep) {
+  const int sh = b - a >= 8 ? 3 : 1;
+  const int g0 = a >> sh, g1 = (b + (1 << sh) - 1) >> sh, gm = g0 + ((g1 - g0 + 1) >> 1);
+  const int lo = half ? max(a, gm << sh) : a, hi = half ? b : min(b, gm << sh);
+  if (lo >= hi) return Acc(0);
+  if (sh == 3) return row_groups<8, V, XT, Acc>(colidx, values, x, f_col, lo, hi, keep);
+  return row_groups<2, V, XT, Acc>(colidx, values, x, f_col, lo, hi, keep);
+}
+
+template <typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_pair_kernel(const int *__restrict__ rows, int n_rows,
+                                                      const int *__restrict__ rowptr,
+                                                      const int *__restrict__ colidx,
+                                                      const V *__restrict__ values,
+                                                      const XT *__restrict__ x, int f_col, XKeep x_keep,
+                                                      Epi epi) {
+  using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
+  typename Epi::State es{};
+  const uint64_t keep = policy_keep(x_keep, x);
+  const int half = threadIdx.x & 1;
+  const unsigned pair = 3u << ((threadIdx.x & 31) & ~1);  // both lanes of a pair always run together
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x) >> 1;
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 1; t < n_rows; t += stride) {
+    const int r = rows ? __ldg(rows + t) : (int)t;
+    const int a = __ldg(rowptr + r), b = __ldg(rowptr + r + 1);
+    const Acc mine = row_half<V, XT, Acc>(colidx, values, x, f_col, a, b, half, keep);
+    const Acc other = __shfl_xor_sync(pair, mine, 1);
+    if (!half) epi.emit(r, mine + other, es);
   }
   epi.block_done(es, blockIdx.x);
 }

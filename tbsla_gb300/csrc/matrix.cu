@@ -423,9 +423,10 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     std::vector<int2> chunk_rows;
     int slot = 0;
     bool all_short = true;
+    int64_t short_nnz = 0;
     for (int r = 0; r < rows; ++r) {
       const int len = rp[r + 1] - rp[r];
-      if (len <= kShortRow) { shorts.push_back(r); continue; }
+      if (len <= kShortRow) { shorts.push_back(r); short_nnz += len; continue; }
       all_short = false;
       if (len <= kChunk) {
         int c = 0;
@@ -444,6 +445,7 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     }
     A->item_class_start[kGroupClasses] = (int)items.size();
     A->n_short = (int)shorts.size();
+    A->short_nnz = short_nnz;
     // staged kernel (all rows short): entries of the largest 32-row tile,
     // rounded up to the 16-entry swizzle group
     A->stage_cap = 0;
@@ -704,10 +706,11 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
     TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0, "PageRank relabel mode %g not -1, 0 or 1", value);
     A->pr_relabel_mode = (int)value;
     return TBSLA_OK;
-  case TBSLA_TUNE_CSR_STAGE:
-    TB_CHECK(value == 0.0 || value == 1.0, "staged kernel mode %g not 0 or 1", value);
-    A->stage_mode = (int)value;
-    if (A->pr_relabel) A->pr_relabel->stage_mode = (int)value;
+  case TBSLA_TUNE_SHORT_ROWS:
+    TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0,
+             "short-row kernel mode %g not -1, 0, 1 or 2", value);
+    A->short_mode = (int)value;
+    if (A->pr_relabel) A->pr_relabel->short_mode = (int)value;
     return TBSLA_OK;
   case TBSLA_TUNE_X_L2_RANGE:
     TB_CHECK(value == 0.0 || value == 1.0, "x L2 range mode %g not 0 or 1", value);

@@ -167,6 +167,7 @@ tbsla_status_t build(tbsla_matrix *A, bool check_skew, bool *built) {
   TB_TRY(tbsla_csr_create(n, n, 0, n, nrp.data(), nci.data(), nva.data(), A->stores, &B));
   B->x_keep = A->x_keep;
   B->x_keep_range = A->x_keep_range;
+  B->short_mode = A->short_mode;
   int *d_newid = nullptr;
   if (cudaMalloc(&d_newid, (size_t)n * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();

@@ -73,7 +73,7 @@ template <typename XT> inline XKeep xkeep_of(const tbsla_matrix *A) {
 // The staged kernel applies when every row is short (stage_cap > 0) and the
 // handle's stage mode (tbsla_matrix_tune) is on.
 inline bool stage_on(const tbsla_matrix *A) {
-  return A->stage_cap > 0 && A->short_rows == nullptr && A->stage_mode > 0 &&
+  return A->stage_cap > 0 && A->short_rows == nullptr && A->short_mode == 1 &&
          A->stage_cap <= kStageCapMax;
 }
 // dynamic shared memory of csr_stage_kernel (the attribute is raised once per
@@ -108,6 +108,15 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
     base += short_grid(A->n_short, Epi::kReduces);
     csr_stage_kernel<V, XT, Epi><<<grid, kStageWarps * 32, smem, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
                                                                      xkeep_of<XT>(A), A->stage_cap, epi);
+  } else if (A->n_short > 0 && (A->short_mode == 2 || (A->short_mode < 0 && sizeof(V) == 8 && !Epi::kReduces &&
+                                                       A->short_nnz >= (int64_t)kPairMinRow * A->n_short))) {
+    // two lanes per row: twice the threads of the one-lane grid (reducing
+    // epilogues: the same capped grid, so every partial slot is written)
+    const int grid = Epi::kReduces ? short_grid(A->n_short, true) : short_grid(2 * A->n_short, false);
+    epi.set_part_base(base);
+    base += short_grid(A->n_short, Epi::kReduces);
+    csr_pair_kernel<V, XT, Epi><<<grid, 256, 0, s>>>(A->short_rows, A->n_short, rowptr, colidx, vals, x, A->f_col,
+                                                     xkeep_of<XT>(A), epi);
   } else if (A->n_short > 0) {
     epi.set_part_base(base);
     base += short_grid(A->n_short, Epi::kReduces);

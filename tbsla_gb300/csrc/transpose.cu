@@ -155,6 +155,7 @@ tbsla_status_t ensure_transpose(tbsla_matrix *A, tbsla_matrix **T) {
   TB_TRY(tbsla_csr_create(ncol, A->n_row, 0, ncol, tp.data(), tci.data(), tva.data(), A->stores, &B));
   B->x_keep = A->x_keep;
   B->x_keep_range = A->x_keep_range;
+  B->short_mode = A->short_mode;
   int *d_perm = nullptr;
   if (cudaMalloc(&d_perm, (size_t)std::max<int64_t>(nnz, 1) * sizeof(int)) != cudaSuccess ||
       (nnz && cudaMemcpy(d_perm, perm.data(), (size_t)nnz * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)) {

@@ -335,8 +335,9 @@ def test_csr_staged_kernel(gpu, orc):
         rp, ci, va = random_csr(rng, nr, nc, lens)
         x = rng.uniform(-1, 1, nc)
         m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
+        m.tune(gpu.TUNE_SHORT_ROWS, 0)
         y0 = m.spmv_host(x)
-        m.tune(gpu.TUNE_CSR_STAGE, 1)
+        m.tune(gpu.TUNE_SHORT_ROWS, 1)
         y1 = m.spmv_host(x)
         assert np.array_equal(y0, y1), f"staged {nr}x{nc}: not bit-identical"
         o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
@@ -345,22 +346,23 @@ def test_csr_staged_kernel(gpu, orc):
         for store in (gpu.F32, gpu.BF16):
             outs = []
             for mode in (0, 1):
-                m.tune(gpu.TUNE_CSR_STAGE, mode)
+                m.tune(gpu.TUNE_SHORT_ROWS, mode)
                 xs = Dev.of(gpu, x.astype(np.float32))
                 ys = Dev(gpu, nr, np.float32)
                 m.spmv_ex(store, gpu.F32, xs.ptr, gpu.F32, ys.ptr)
                 outs.append(ys.get())
             assert np.array_equal(outs[0], outs[1]), f"staged store {store} {nr}x{nc}"
         if nr == nc:
-            m.tune(gpu.TUNE_CSR_STAGE, 0)
+            m.tune(gpu.TUNE_SHORT_ROWS, 0)
             r0 = m.a_axpx_host(x)
-            m.tune(gpu.TUNE_CSR_STAGE, 1)
+            m.tune(gpu.TUNE_SHORT_ROWS, 1)
             assert np.array_equal(r0, m.a_axpx_host(x)), "staged a_axpx"
     # PageRank sweeps (reducing epilogue) on a column-stochastic cqmat
     g = gpu.generate("CSR", "cqmat_stochastic", 50000, 50000, 12, 0.1, 2)
     m = gpu.DeviceMatrix.from_generated(g)
+    m.tune(gpu.TUNE_SHORT_ROWS, 0)
     x0, r0 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
-    m.tune(gpu.TUNE_CSR_STAGE, 1)
+    m.tune(gpu.TUNE_SHORT_ROWS, 1)
     x1, r1 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
     # the per-block partial sums group rows differently: equal to rounding
     assert abs(r0.iterations - r1.iterations) <= 1 and r1.converged
@@ -383,3 +385,38 @@ def test_l2_fetch_granularity(gpu):
         ys.append(m.spmv_host(x))
     assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[0], ys[2])
     assert L.tbsla_set_l2_fetch_granularity(48) != 0
+
+
+def test_csr_pair_kernel(gpu, orc):
+    """Two lanes per short row (TBSLA_TUNE_SHORT_ROWS = 2): each lane sums half
+    the row in stored order, the row is the halves' sum -- within the FP64
+    bound of the oracle on uniform, ragged and skewed matrices (short rows
+    listed among long ones), for reduced-precision stores, a_axpx and the
+    PageRank sweep epilogue."""
+    rng = np.random.default_rng(41)
+    skew = rng.zipf(1.5, 30000).clip(0, 20000)
+    skew[:5] = 0
+    cases = [(20000, 20000, np.full(20000, 16)), (20011, 5000, rng.integers(0, 33, 20011)),
+             (30000, 30000, skew), (33, 40, rng.integers(0, 4, 33)), (1, 7, np.array([5]))]
+    for (nr, nc, lens) in cases:
+        rp, ci, va = random_csr(rng, nr, nc, lens)
+        x = rng.uniform(-1, 1, nc)
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32)
+        m.tune(gpu.TUNE_SHORT_ROWS, 2)
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+        sc = so.spmv(np.abs(x))
+        assert_close(m.spmv_host(x), o.spmv(x), sc, RTOL64, f"pairs {nr}x{nc}")
+        xs = Dev.of(gpu, x.astype(np.float32))
+        ys = Dev(gpu, nr, np.float32)
+        m.spmv_ex(gpu.F32, gpu.F32, xs.ptr, gpu.F32, ys.ptr)
+        assert_close(ys.get().astype(np.float64), o.spmv(x), sc, 2e-6, f"pairs F32 {nr}x{nc}")
+        if nr == nc:
+            assert_close(m.a_axpx_host(x), o.a_axpx(x), so.spmv(sc + np.abs(x)), RTOL64, "pairs a_axpx")
+    g = gpu.generate("CSR", "cqmat_stochastic", 50000, 50000, 12, 0.1, 2)
+    m = gpu.DeviceMatrix.from_generated(g)
+    x0, r0 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
+    m.tune(gpu.TUNE_SHORT_ROWS, 2)
+    x1, r1 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
+    assert abs(r0.iterations - r1.iterations) <= 1 and r1.converged
+    assert float(np.abs(x0 - x1).sum()) <= 1e-11
