@@ -195,9 +195,27 @@ __device__ __forceinline__ float fma_acc(float a, float b, float c) { return __f
 
 // streaming loads of matrix data (read once: evict-first in L2 so that the
 // gathered vector stays resident)
-template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
+// (256-byte L2 prefetches: streams stay wide when the process lowers the L2
+// fetch granularity for gathers, tbsla_set_l2_fetch_granularity)
+template <typename T> __device__ __forceinline__ T ld_stream(const T *p);
+template <> __device__ __forceinline__ double ld_stream(const double *p) {
+  double v;
+  asm("ld.global.cs.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+template <> __device__ __forceinline__ float ld_stream(const float *p) {
+  float v;
+  asm("ld.global.cs.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+template <> __device__ __forceinline__ int ld_stream(const int *p) {
+  int v;
+  asm("ld.global.cs.L2::256B.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
 template <> __device__ __forceinline__ __nv_bfloat16 ld_stream(const __nv_bfloat16 *p) {
-  unsigned short u = __ldcs(reinterpret_cast<const unsigned short *>(p));
+  unsigned short u;
+  asm("ld.global.cs.L2::256B.u16 %0, [%1];" : "=h"(u) : "l"(p));
   return __ushort_as_bfloat16(u);
 }
 
