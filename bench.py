@@ -3,8 +3,8 @@
 Headline (``value``): CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24, c = 16,
 q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of algorithmic traffic per
 product), in GB/s of algorithmic bytes over device time with the matrix and x
-resident in HBM, run with 32-byte L2 fetches (tbsla_set_l2_fetch_granularity;
-the other sections at 128).  A "step" is one product.  ``e2e`` is the same metric through
+resident in HBM.  Every section runs with 32-byte L2 fetches
+(tbsla_set_l2_fetch_granularity).  A "step" is one product.  ``e2e`` is the same metric through
 the C ABI's host-vector call (tbsla_spmv_host) on pinned host vectors: x is
 copied into HBM and the product writes y into host memory over NVLink-C2C,
 both inside the timed region.
@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 N_HEADLINE = 1 << 24
 C_HEADLINE = 16
 Q_HEADLINE = 0.1
-L2_FETCH_HEADLINE = 32  # bytes (tbsla_set_l2_fetch_granularity)
+L2_FETCH_BYTES = 32  # L2 fetch granularity of the whole run (tbsla_set_l2_fetch_granularity)
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
@@ -504,10 +504,9 @@ def run_gb300(args, world, rank, local, pg):
     torch.cuda.set_device(local)
 
     n = 1 << args.log2n
-    # the headline product runs with 32-byte L2 fetches (the random gathers of
-    # x bring one sector; the kernel's streams ask for 256-byte prefetches);
-    # the other sections run at 128, the context default's behaviour
-    capi.check(L.tbsla_set_l2_fetch_granularity(L2_FETCH_HEADLINE))
+    # every section runs with 32-byte L2 fetches: the random gathers of x
+    # bring one sector, the kernels' streams ask for 256-byte prefetches
+    capi.check(L.tbsla_set_l2_fetch_granularity(L2_FETCH_BYTES))
     t0 = time.time()
     g = capi.generate("CSR", "cqmat", n, n, C_HEADLINE, Q_HEADLINE, 0)
     A = capi.DeviceMatrix.from_generated(g)
@@ -562,7 +561,6 @@ def run_gb300(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
     L.tbsla_host_free(hx)
     L.tbsla_host_free(hy)
-    capi.check(L.tbsla_set_l2_fetch_granularity(128))
     A.close()
     torch.cuda.empty_cache()
 
@@ -582,7 +580,7 @@ def run_gb300(args, world, rank, local, pg):
                    "algorithmic_bytes": algo,
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: 3.56 GB streamed per step, no flush needed",
-                   "l2_fetch_granularity_bytes": L2_FETCH_HEADLINE},
+                   "l2_fetch_granularity_bytes": L2_FETCH_BYTES},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": NCU_TRAFFIC_BYTES if args.log2n == 24 else None,
@@ -621,6 +619,7 @@ def main():
     if args.pagerank_only or args.section:
         from tbsla_gb300 import build, capi
         build.build()
+        capi.check(capi.lib().tbsla_set_l2_fetch_granularity(L2_FETCH_BYTES))
         if args.pagerank_only or args.section == "pagerank":
             print(json.dumps({"pagerank": pagerank_bench(capi, args.rmat_scale)}), flush=True)
         elif args.section == "batching":

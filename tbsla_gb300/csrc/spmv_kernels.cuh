@@ -253,9 +253,35 @@ template <typename V> struct Vec4 { V v[4]; };
 // Streaming (.cs, evict-first) loads when x stays in L2; default loads when
 // x is larger than L2, where evict-first row data measured slower (ELL FP64
 // cqmat 2^24: 3.6 vs 4.0 TB/s; 2^22: 5.95 vs 5.68 TB/s).
-template <bool CS, typename T> __device__ __forceinline__ T ld_row(const T *p) {
-  if constexpr (CS) return __ldcs(p);
-  else return __ldg(p);
+// ELL row data: streaming (.cs) or read-only loads, both asking for 256-byte
+// L2 prefetches (streams stay wide at a 32-byte L2 fetch granularity)
+template <bool CS> __device__ __forceinline__ double2 ld_row(const double2 *p) {
+  double2 v;
+  if constexpr (CS) asm("ld.global.cs.L2::256B.v2.f64 {%0,%1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  else asm("ld.global.nc.L2::256B.v2.f64 {%0,%1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
+template <bool CS> __device__ __forceinline__ float4 ld_row(const float4 *p) {
+  float4 v;
+  if constexpr (CS)
+    asm("ld.global.cs.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  else
+    asm("ld.global.nc.L2::256B.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  return v;
+}
+template <bool CS> __device__ __forceinline__ uint2 ld_row(const uint2 *p) {
+  uint2 v;
+  if constexpr (CS) asm("ld.global.cs.L2::256B.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+  else asm("ld.global.nc.L2::256B.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+  return v;
+}
+template <bool CS> __device__ __forceinline__ int4 ld_row(const int4 *p) {
+  int4 v;
+  if constexpr (CS)
+    asm("ld.global.cs.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+  else
+    asm("ld.global.nc.L2::256B.v4.s32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+  return v;
 }
 
 template <typename V, bool CS = true> __device__ __forceinline__ Vec4<V> ld4(const V *p) {
