@@ -4,7 +4,8 @@ Headline (``value``): CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24, c = 16
 q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of algorithmic traffic per
 product), in GB/s of algorithmic bytes over device time with the matrix and x
 resident in HBM.  Every section runs with 32-byte L2 fetches
-(tbsla_set_l2_fetch_granularity).  A "step" is one product.  ``e2e`` is the same metric through
+(tbsla_set_l2_fetch_granularity); the headline keeps x evict-last in a 64 MiB
+persisting L2 set-aside (tbsla_set_l2_persisting).  A "step" is one product.  ``e2e`` is the same metric through
 the C ABI's host-vector call (tbsla_spmv_host) on pinned host vectors: x is
 copied into HBM and the product writes y into host memory over NVLink-C2C,
 both inside the timed region.
@@ -44,12 +45,14 @@ N_HEADLINE = 1 << 24
 C_HEADLINE = 16
 Q_HEADLINE = 0.1
 L2_FETCH_BYTES = 32  # L2 fetch granularity of the whole run (tbsla_set_l2_fetch_granularity)
+L2_PERSIST_BYTES = 64 << 20  # persisting L2 set-aside of the headline (tbsla_set_l2_persisting)
+X_KEEP_HEADLINE = 1.0  # fraction of x loaded evict-last in the headline (TBSLA_TUNE_X_L2_KEEP)
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
 # workload, from the ncu capture summarised in
 # profiles/csr_pair_kernel_cqmat_2p24.md
-NCU_TRAFFIC_BYTES = 4_128_661_388
+NCU_TRAFFIC_BYTES = 3_986_563_910
 
 
 def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):
@@ -507,9 +510,18 @@ def run_gb300(args, world, rank, local, pg):
     # every section runs with 32-byte L2 fetches: the random gathers of x
     # bring one sector, the kernels' streams ask for 256-byte prefetches
     capi.check(L.tbsla_set_l2_fetch_granularity(L2_FETCH_BYTES))
+    # the headline (device and end-to-end products) keeps all of x evict-last
+    # in a 64 MiB persisting L2 set-aside; the context's set-aside is restored
+    # after it (PageRank sweeps lose 2 % with the larger one)
+    sa0, sa_max = C.c_size_t(), C.c_size_t()
+    capi.check(L.tbsla_get_l2_persisting(C.byref(sa0), C.byref(sa_max)))
+    capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
+    sa_set = C.c_size_t()
+    capi.check(L.tbsla_get_l2_persisting(C.byref(sa_set), None))
     t0 = time.time()
     g = capi.generate("CSR", "cqmat", n, n, C_HEADLINE, Q_HEADLINE, 0)
     A = capi.DeviceMatrix.from_generated(g)
+    A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_HEADLINE)
     setup_s = time.time() - t0
     nnz = int(g.values.size)
     algo = csr_bytes(n, n, nnz)
@@ -561,6 +573,7 @@ def run_gb300(args, world, rank, local, pg):
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
     L.tbsla_host_free(hx)
     L.tbsla_host_free(hy)
+    capi.check(L.tbsla_set_l2_persisting(sa0.value))
     A.close()
     torch.cuda.empty_cache()
 
@@ -580,7 +593,8 @@ def run_gb300(args, world, rank, local, pg):
                    "algorithmic_bytes": algo,
                    "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2: 3.56 GB streamed per step, no flush needed",
-                   "l2_fetch_granularity_bytes": L2_FETCH_BYTES},
+                   "l2_fetch_granularity_bytes": L2_FETCH_BYTES,
+                   "l2_persisting_bytes": int(sa_set.value), "x_evict_last_fraction": X_KEEP_HEADLINE},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": NCU_TRAFFIC_BYTES if args.log2n == 24 else None,

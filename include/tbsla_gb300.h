@@ -87,6 +87,18 @@ tbsla_status_t tbsla_set_device(int device);
  * at 32; the setting is the caller's, process-wide, and ends with it. */
 tbsla_status_t tbsla_set_l2_fetch_granularity(int bytes);
 tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes);
+/* The current device's persisting L2 set-aside for this process (the CUDA
+ * context limit cudaLimitPersistingL2CacheSize; the device rounds it, and
+ * reports its maximum in *max_bytes).  Lines loaded with an evict-last
+ * policy -- the gathered x, TBSLA_TUNE_X_L2_KEEP -- stay there ahead of the
+ * streamed matrix.  cqmat 2^24 FP64 with all of x evict-last: 5085 GB/s at
+ * 64 MiB against 4811 at the context's default (25 MB here); the maximum
+ * (84 MB) leaves the streams too little L2 (2920 GB/s), and R-MAT PageRank
+ * sweeps lose 2 % at 64 MiB.  Setting it first returns every persisting
+ * line to normal (cudaCtxResetPersistingL2Cache).  Process-wide, the
+ * caller's to set and restore. */
+tbsla_status_t tbsla_set_l2_persisting(size_t bytes);
+tbsla_status_t tbsla_get_l2_persisting(size_t *bytes, size_t *max_bytes);
 
 /* ------------------------------------------------------------ matrices */
 /* CSR from host arrays.  Replaces MatrixCSR(n_row, n_col, values, rowptr,

@@ -134,6 +134,8 @@ def lib() -> C.CDLL:
         "tbsla_coo_to_scoo": ([P, C.c_int, C.POINTER(P)], st),
         "tbsla_set_l2_fetch_granularity": ([C.c_int], st),
         "tbsla_get_l2_fetch_granularity": ([C.POINTER(C.c_int)], st),
+        "tbsla_set_l2_persisting": ([C.c_size_t], st),
+        "tbsla_get_l2_persisting": ([C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], st),
         "tbsla_csr_normalize_columns": ([P, _vp], st),
         "tbsla_ell_download": ([P, _vp, _vp], st),
         "tbsla_dense_download": ([P, _vp], st),

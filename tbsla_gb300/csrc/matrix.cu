@@ -526,6 +526,24 @@ tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes) {
   return TBSLA_OK;
 }
 
+tbsla_status_t tbsla_set_l2_persisting(size_t bytes) {
+  TB_CUDA(cudaSetDevice(current_device()));
+  TB_CUDA(cudaCtxResetPersistingL2Cache());
+  TB_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes));
+  return TBSLA_OK;
+}
+
+tbsla_status_t tbsla_get_l2_persisting(size_t *bytes, size_t *max_bytes) {
+  TB_CUDA(cudaSetDevice(current_device()));
+  if (bytes) TB_CUDA(cudaDeviceGetLimit(bytes, cudaLimitPersistingL2CacheSize));
+  if (max_bytes) {
+    int v = 0;
+    TB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxPersistingL2CacheSize, current_device()));
+    *max_bytes = (size_t)v;
+  }
+  return TBSLA_OK;
+}
+
 tbsla_status_t tbsla_set_device(int device) {
   int n = 0;
   TB_CUDA(cudaGetDeviceCount(&n));

@@ -420,3 +420,26 @@ def test_csr_pair_kernel(gpu, orc):
     x1, r1 = m.pagerank_host(beta=0.85, tol=1e-12, max_iter=500, mode=gpu.PR_DANGLING)
     assert abs(r0.iterations - r1.iterations) <= 1 and r1.converged
     assert float(np.abs(x0 - x1).sum()) <= 1e-11
+
+
+def test_l2_persisting_setaside(gpu):
+    """The process's persisting L2 set-aside is set, read back (rounded by the
+    device, within its maximum) and restored; products do not depend on it or
+    on the evict-last fraction of x."""
+    L = gpu.lib()
+    cur, mx = C.c_size_t(), C.c_size_t()
+    gpu.check(L.tbsla_get_l2_persisting(C.byref(cur), C.byref(mx)))
+    assert mx.value > 0
+    g = gpu.generate("CSR", "cqmat", 30000, 30000, 16, 0.1, 0)
+    m = gpu.DeviceMatrix.from_generated(g)
+    x = np.random.default_rng(5).uniform(-1, 1, 30000)
+    y0 = m.spmv_host(x)
+    for want in (0, 32 << 20, mx.value):
+        gpu.check(L.tbsla_set_l2_persisting(want))
+        got = C.c_size_t()
+        gpu.check(L.tbsla_get_l2_persisting(C.byref(got), None))
+        assert got.value <= mx.value and (want == 0) == (got.value == 0)
+        for keep in (0.0, 1.0):
+            m.tune(gpu.TUNE_X_L2_KEEP, keep)
+            assert np.array_equal(m.spmv_host(x), y0)
+    gpu.check(L.tbsla_set_l2_persisting(cur.value))
