@@ -284,13 +284,14 @@ def pagerank_bench(capi, scale=24):
            "edges": int(info.stored), "setup_s": round(setup, 1), "tol": 1e-10,
            "reference_solve": {"tol": 1e-13, "sweeps": r.iterations, "converged": bool(r.converged)}}
     times = {}
-    for name, prec in (("fp64", capi.F64), ("fp32_refined", capi.F32), ("bf16_refined", capi.BF16)):
-        A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec)  # warm: workspace + graphs
+    for name, prec, acc in (("fp64", capi.F64, 0), ("fp32_refined", capi.F32, 0), ("bf16_refined", capi.BF16, 0),
+                            ("fp64_anderson", capi.F64, 1)):
+        A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec, accel=acc)  # warm: workspace + graphs
         torch.cuda.synchronize()
         ts = []
         for _ in range(3):
             t1 = time.perf_counter()
-            r = A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec)
+            r = A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec, accel=acc)
             torch.cuda.synchronize()
             ts.append(time.perf_counter() - t1)
         err = float((out - ref).abs().sum().item())
@@ -298,6 +299,7 @@ def pagerank_bench(capi, scale=24):
         res[name] = {"ms": round(min(ts) * 1e3, 2), "sweeps": r.iterations, "fp64_sweeps": r.iterations_f64,
                      "residual": r.residual, "converged": bool(r.converged), "l1_vs_fp64_1e-13": err}
     res["bf16_over_fp64_time"] = round(times["bf16_refined"] / times["fp64"], 3)
+    res["anderson_over_fp64_time"] = round(times["fp64_anderson"] / times["fp64"], 3)
     res["fp32_over_fp64_time"] = round(times["fp32_refined"] / times["fp64"], 3)
     A.close()
     torch.cuda.empty_cache()

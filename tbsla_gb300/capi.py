@@ -43,7 +43,7 @@ class MatrixInfo(C.Structure):
 
 class PageRankParams(C.Structure):
     _fields_ = [("beta", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int), ("mode", C.c_int),
-                ("precision", C.c_int), ("check_every", C.c_int)]
+                ("precision", C.c_int), ("check_every", C.c_int), ("accel", C.c_int)]
 
 
 class AutotuneResult(C.Structure):
@@ -330,8 +330,8 @@ class DeviceMatrix:
 
     # -- PageRank --------------------------------------------------------
     def pagerank_host(self, beta=0.85, tol=1e-10, max_iter=10000, mode=PR_DANGLING, precision=F64,
-                      check_every=0):
-        p = PageRankParams(beta, tol, max_iter, mode, precision, check_every)
+                      check_every=0, accel=0):
+        p = PageRankParams(beta, tol, max_iter, mode, precision, check_every, accel)
         r = PageRankResult()
         n = self.info().n_col
         out = np.zeros(max(n, 1), np.float64)
@@ -339,8 +339,8 @@ class DeviceMatrix:
         return out[:n], r
 
     def pagerank(self, d_out: int, beta=0.85, tol=1e-10, max_iter=10000, mode=PR_DANGLING, precision=F64,
-                 check_every=0, stream: int | None = None):
-        p = PageRankParams(beta, tol, max_iter, mode, precision, check_every)
+                 check_every=0, stream: int | None = None, accel=0):
+        p = PageRankParams(beta, tol, max_iter, mode, precision, check_every, accel)
         r = PageRankResult()
         check(lib().tbsla_pagerank(self.h, C.byref(p), d_out, C.byref(r), stream))
         return r

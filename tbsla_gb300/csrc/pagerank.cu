@@ -18,6 +18,9 @@
 //     Matrix::personalized_page_rank (Matrix.cpp:63-114).
 //   TBSLA_PR_DANGLING   x = beta*A x + (beta*dangling(x) + (1-beta)*sum(x))/n,
 //     stop when ||x - x_prev||_1 < tol.
+//   accelerated (DANGLING, FP64, accel = 1): Anderson acceleration of the
+//     same fixed-point map over the last two differences (pr_aa_*), same
+//     stopping rule on ||G(x) - x||_1, the result is G(x) of the last sweep.
 //   mixed precision (DANGLING, precision F32/BF16): FP64 defect correction.
 //     r = G(x) - x by an FP64 sweep (its L1 norm is the stopping quantity),
 //     then e_{j+1} = G~ e_j + r by sweeps on the reduced-precision value store
@@ -43,6 +46,14 @@ struct PrCtl {
   double inner_resid, inner_tol;
   int iter, done, converged, max_iter;
   int inner_iter, inner_done, inner_max, pad;
+  // Anderson acceleration (FP64 dangling mode): dangling mass and sum of the
+  // last three sweep outputs (slot k % 3), their residuals' Gram matrix with
+  // the newest first (gram[i][j] = r_{k-i} . r_{k-j}), and the coefficients
+  // of the next input in the newest-first outputs
+  double aa_d[3], aa_s[3];
+  double gram[3][3];
+  double coef[3];
+  int aa_m, aa_pad;
 };
 
 enum { kSweepRef = 0, kSweepDang = 1, kSweepInner = 2, kSweepTele = 3 };
@@ -209,7 +220,7 @@ __global__ void __launch_bounds__(256) pr_normalize_kernel(double *__restrict__ 
 __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restrict__ partials, int nparts,
                                                           PrCtl *ctl, int stage) {
   const bool inner = stage == 3;
-  if ((stage <= 3 || stage == 8 || stage == 10) &&
+  if ((stage <= 3 || stage == 8 || stage == 10 || stage == 12 || stage == 13) &&
       (inner ? *(volatile int *)&ctl->inner_done : *(volatile int *)&ctl->done))
     return;
   __shared__ double sh[3][256];
@@ -297,6 +308,106 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
   case 11:  // initial adjoint vector: b = v . lambda0
     ctl->add = ctl->beta * b;
     break;
+  case 12: {  // accelerated sweep k: resid = a, dangling mass b and sum c of g_k
+    const int slot = ctl->iter % 3;
+    ctl->resid = a;
+    ctl->aa_d[slot] = b;
+    ctl->aa_s[slot] = c;
+    ctl->d = b;
+    ctl->s = c;
+    ctl->iter += 1;
+    ctl->converged = a < ctl->tol;
+    ctl->done = ctl->converged || ctl->iter >= ctl->max_iter;
+    break;
+  }
+  case 13:  // residual dots of sweep k: r_k . r_k, r_k . r_{k-1}, r_k . r_{k-2}
+    // shift the newest-first Gram matrix by one and add the new row
+    ctl->gram[2][2] = ctl->gram[1][1];
+    ctl->gram[1][2] = ctl->gram[2][1] = ctl->gram[0][1];
+    ctl->gram[1][1] = ctl->gram[0][0];
+    ctl->gram[0][0] = a;
+    ctl->gram[0][1] = ctl->gram[1][0] = b;
+    ctl->gram[0][2] = ctl->gram[2][0] = c;
+    break;
+  }
+}
+
+// The Anderson step after sweep k (one thread): with q_j = r_{k-j}, minimise
+// || q_0 - g1 (q_0 - q_1) - g2 (q_1 - q_2) ||_2 over the available history
+// (normal equations from the Gram matrix), then the next input is
+// x_{k+1} = (1 - g1) g_k + (g1 - g2) g_{k-1} + g2 g_{k-2}.  Its dangling
+// mass and sum follow from the outputs' (linear), which gives the next
+// sweep's teleport term.  Ill-conditioned systems or large coefficients fall
+// back to fewer differences, down to the plain step x_{k+1} = g_k.
+__global__ void pr_aa_solve_kernel(PrCtl *ctl) {
+  if (*(volatile int *)&ctl->done) return;
+  const int k = ctl->iter - 1;        // the sweep just finished
+  int m = k < 2 ? k : 2;              // differences available
+  const double(&G)[3][3] = ctl->gram;
+  double g1 = 0, g2 = 0;
+  if (m == 2) {
+    const double a11 = G[0][0] - 2 * G[0][1] + G[1][1];
+    const double a12 = G[0][1] - G[0][2] - G[1][1] + G[1][2];
+    const double a22 = G[1][1] - 2 * G[1][2] + G[2][2];
+    const double b1 = G[0][0] - G[0][1], b2 = G[0][1] - G[0][2];
+    const double det = a11 * a22 - a12 * a12;
+    if (det > 1e-12 * a11 * a22 && a11 > 0 && a22 > 0) {
+      g1 = (b1 * a22 - b2 * a12) / det;
+      g2 = (a11 * b2 - a12 * b1) / det;
+    } else {
+      m = 1;
+    }
+    if (m == 2 && !(fabs(g1) < 8.0 && fabs(g2) < 8.0)) { g1 = g2 = 0; m = 1; }
+  }
+  if (m == 1) {
+    const double a11 = G[0][0] - 2 * G[0][1] + G[1][1], b1 = G[0][0] - G[0][1];
+    g1 = a11 > 0 ? b1 / a11 : 0.0;
+    g2 = 0;
+    if (!(fabs(g1) < 8.0)) g1 = 0;
+  }
+  const double c0 = 1.0 - g1, c1 = g1 - g2, c2 = g2;
+  ctl->coef[0] = c0;
+  ctl->coef[1] = c1;
+  ctl->coef[2] = c2;
+  ctl->aa_m = (c1 != 0.0 || c2 != 0.0) ? (c2 != 0.0 ? 2 : 1) : 0;
+  const int s0 = k % 3, s1 = (k + 2) % 3, s2 = (k + 1) % 3;  // slots of g_k, g_{k-1}, g_{k-2}
+  double d = c0 * ctl->aa_d[s0], sum = c0 * ctl->aa_s[s0];
+  if (ctl->aa_m >= 1) { d += c1 * ctl->aa_d[s1]; sum += c1 * ctl->aa_s[s1]; }
+  if (ctl->aa_m >= 2) { d += c2 * ctl->aa_d[s2]; sum += c2 * ctl->aa_s[s2]; }
+  ctl->add = (ctl->beta * d + (1.0 - ctl->beta) * sum) * ctl->inv_n;
+}
+
+// r_k = g_k - x_k into its slot, and the partial dots of r_k with r_k,
+// r_{k-1}, r_{k-2} (the missing ones are 0)
+__global__ void __launch_bounds__(256) pr_aa_dots_kernel(const double *__restrict__ g, const double *__restrict__ x,
+                                                         double *__restrict__ r0, const double *__restrict__ r1,
+                                                         const double *__restrict__ r2, int n, const PrCtl *ctl,
+                                                         double *partials) {
+  if (*(volatile const int *)&ctl->done) return;
+  const int k = ctl->iter - 1;
+  double p0 = 0, p1 = 0, p2 = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double r = g[i] - x[i];
+    r0[i] = r;
+    p0 += r * r;
+    if (k >= 1) p1 += r * r1[i];
+    if (k >= 2) p2 += r * r2[i];
+  }
+  block_reduce3(p0, p1, p2, false, partials, blockIdx.x);
+}
+
+// x_{k+1} = c0 g_k + c1 g_{k-1} + c2 g_{k-2} (only the terms in use are read)
+__global__ void __launch_bounds__(256) pr_aa_combine_kernel(const double *__restrict__ g0, const double *__restrict__ g1,
+                                                            const double *__restrict__ g2, double *__restrict__ x, int n,
+                                                            const PrCtl *ctl) {
+  if (*(volatile const int *)&ctl->done) return;
+  const double c0 = ctl->coef[0], c1 = ctl->coef[1], c2 = ctl->coef[2];
+  const int m = ctl->aa_m;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = c0 * g0[i];
+    if (m >= 1) v = fma(c1, g1[i], v);
+    if (m >= 2) v = fma(c2, g2[i], v);
+    x[i] = v;
   }
 }
 
@@ -367,6 +478,8 @@ struct PrWork {
   unsigned char *dmask = nullptr, *tmask = nullptr;
   double *tvec = nullptr;             // teleport mode: copy of the teleport vector
   double *lam[2] = {nullptr, nullptr};  // adjoint iterates
+  double *ag[3] = {nullptr, nullptr, nullptr};  // accelerated solve: sweep outputs (slot k % 3)
+  double *ar[3] = {nullptr, nullptr, nullptr};  // and their residuals
   double *adj_partials = nullptr;
   int adj_nparts = 0;
   double *partials = nullptr;
@@ -381,7 +494,7 @@ struct PrWork {
   ~PrWork() {
     for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
     void *ps[] = {x[0], x[1], prod, e[0], e[1], prod32, r, dmask, tmask, tvec, lam[0], lam[1], adj_partials,
-                  partials, ctl};
+                  partials, ctl, ag[0], ag[1], ag[2], ar[0], ar[1], ar[2]};
     for (void *p : ps) if (p) cudaFree(p);
     if (ctl_host) cudaFreeHost(ctl_host);
     if (stream) cudaStreamDestroy(stream);
@@ -479,7 +592,7 @@ static tbsla_status_t pr_inner_buffers(PrWork *W) {
 
 // one FP64 sweep x_in -> x_out (mode kSweepRef or kSweepDang) + finalize
 static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const double *x_in, double *x_out,
-                                        int mode, bool with_tmask, cudaStream_t s) {
+                                        int mode, bool with_tmask, cudaStream_t s, bool accel = false) {
   PrEpi<double, double> epi{};
   epi.y = x_out;
   epi.xold = x_in;
@@ -508,8 +621,23 @@ static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const 
     pr_normalize_kernel<<<kAffineBlocks, 256, 0, s>>>(x_out, x_in, W->n, W->ctl, W->partials);
     pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 1);
   } else {
-    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, mode == kSweepTele ? 8 : 2);
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, accel ? 12 : mode == kSweepTele ? 8 : 2);
   }
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// one accelerated iteration k (slot k % 3): g_k = G(x), residual dots, the
+// Anderson step, x <- the combination
+static tbsla_status_t enqueue_aa_iteration(const tbsla_matrix *A, PrWork *W, int k, cudaStream_t s) {
+  const int s0 = k % 3, s1 = (k + 2) % 3, s2 = (k + 1) % 3;
+  double *x = W->x[0];
+  TB_TRY(enqueue_f64_sweep(A, W, x, W->ag[s0], kSweepDang, false, s, true));
+  pr_aa_dots_kernel<<<kAffineBlocks, 256, 0, s>>>(W->ag[s0], x, W->ar[s0], W->ar[s1], W->ar[s2], W->n, W->ctl,
+                                                  W->partials);
+  pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 13);
+  pr_aa_solve_kernel<<<1, 1, 0, s>>>(W->ctl);
+  pr_aa_combine_kernel<<<kAffineBlocks, 256, 0, s>>>(W->ag[s0], W->ag[s1], W->ag[s2], x, W->n, W->ctl);
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
 }
@@ -547,8 +675,9 @@ static tbsla_status_t enqueue_inner_sweep(const tbsla_matrix *A, PrWork *W, tbsl
 }
 
 // A graph of `sweeps` sweeps (kind 0: FP64 sweeps from x[0], alternating;
-// kind 1: inner sweeps from e[0], alternating); sweeps is even so that the
-// buffers are back in place after each launch.
+// kind 1: inner sweeps from e[0], alternating; kind 2: accelerated
+// iterations, slots k % 3); sweeps is even (kind 2: a multiple of 6) so that
+// the buffers are back in place after each launch.
 static tbsla_status_t get_graph(const tbsla_matrix *A, PrWork *W, int kind, int sweeps, int precision, int mode,
                                 bool with_tmask, cudaGraphExec_t *exec) {
   for (auto &g : W->graphs)
@@ -561,7 +690,8 @@ static tbsla_status_t get_graph(const tbsla_matrix *A, PrWork *W, int kind, int 
   tbsla_status_t st = TBSLA_OK;
   for (int k = 0; k < sweeps && st == TBSLA_OK; ++k) {
     if (kind == 0) st = enqueue_f64_sweep(A, W, W->x[k & 1], W->x[(k + 1) & 1], mode, with_tmask, s);
-    else st = enqueue_inner_sweep(A, W, (tbsla_dtype_t)precision, W->e[k & 1], W->e[(k + 1) & 1], s);
+    else if (kind == 1) st = enqueue_inner_sweep(A, W, (tbsla_dtype_t)precision, W->e[k & 1], W->e[(k + 1) & 1], s);
+    else st = enqueue_aa_iteration(A, W, k, s);
   }
   cudaGraph_t graph = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -599,6 +729,24 @@ static tbsla_status_t run_f64(tbsla_matrix *A, PrWork *W, int mode, bool with_tm
   return TBSLA_OK;
 }
 
+// the Anderson-accelerated FP64 solve (dangling mode); result in ag[(iter-1) % 3]
+static tbsla_status_t run_aa(tbsla_matrix *A, PrWork *W, int check_every) {
+  if (!W->ag[0])
+    for (int i = 0; i < 3; ++i) {
+      TB_TRY(pr_alloc((void **)&W->ag[i], (size_t)W->n * 8));
+      TB_TRY(pr_alloc((void **)&W->ar[i], (size_t)W->n * 8));
+    }
+  const int K = std::max(6, (check_every + 5) / 6 * 6);
+  cudaGraphExec_t ex;
+  TB_TRY(get_graph(A, W, 2, K, TBSLA_F64, kSweepDang, false, &ex));
+  while (true) {
+    TB_CUDA(cudaGraphLaunch(ex, W->stream));
+    TB_TRY(read_ctl(W));
+    if (W->ctl_host->done) break;
+  }
+  return TBSLA_OK;
+}
+
 static double *pr_result(PrWork *W) { return W->result; }
 
 tbsla_status_t pr_relabelled(tbsla_matrix *A, tbsla_matrix **B);
@@ -621,6 +769,8 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
            "the teleport mode needs a teleport vector and FP64");
   TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32 || p->precision == TBSLA_BF16, "bad precision");
   TB_CHECK(p->precision == TBSLA_F64 || p->mode == TBSLA_PR_DANGLING, "reduced precision needs TBSLA_PR_DANGLING");
+  TB_CHECK(p->accel == 0 || (p->accel == 1 && p->precision == TBSLA_F64 && p->mode == TBSLA_PR_DANGLING),
+           "accel = %d: Anderson acceleration (1) is for TBSLA_PR_DANGLING in FP64", p->accel);
   TB_CHECK(A->values[0], "PageRank needs the F64 value store");
   TB_CHECK(p->precision == TBSLA_F64 || A->values[store_index((tbsla_dtype_t)p->precision)],
            "the requested reduced-precision value store is not present");
@@ -684,7 +834,12 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   TB_CUDA(cudaGetLastError());
 
   int f64_sweeps = 0, inner_total = 0;
-  if (p->precision == TBSLA_F64) {
+  const bool accel = p->accel != 0 && p->precision == TBSLA_F64 && p->mode == TBSLA_PR_DANGLING;
+  if (accel) {
+    if (!c.done) TB_TRY(run_aa(A, W, K));
+    else TB_TRY(read_ctl(W));
+    f64_sweeps = c.iter;
+  } else if (p->precision == TBSLA_F64) {
     const int sweep = p->mode == TBSLA_PR_REFERENCE ? kSweepRef : p->mode == TBSLA_PR_TELEPORT ? kSweepTele : kSweepDang;
     if (!c.done) TB_TRY(run_f64(A, W, sweep, with_tmask, K));
     else TB_TRY(read_ctl(W));
@@ -725,7 +880,8 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   }
   // result buffer: FP64 runs end in x[iter % 2]; the mixed run in x[1], the
   // output G(x) of its last FP64 sweep
-  W->result = p->precision == TBSLA_F64 ? W->x[c.iter & 1] : W->x[1];
+  W->result = accel ? (c.iter > 0 ? W->ag[(c.iter - 1) % 3] : W->x[0])
+                    : p->precision == TBSLA_F64 ? W->x[c.iter & 1] : W->x[1];
   double *xr = W->result;
   if (p->mode == TBSLA_PR_REFERENCE || p->precision != TBSLA_F64) {
     // reference: b /= sum(b) (Matrix.cpp:52-59); mixed: sum-normalise

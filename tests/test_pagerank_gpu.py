@@ -96,12 +96,21 @@ def test_dangling_mode_fp64_and_mixed(gpu, orc, scale):
     x8o, _, _ = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 0.0, 8)
     x8o = x8o / math.fsum(x8o)
     assert r8.iterations == 8 and np.abs(x8 - x8o).sum() < 1e-13
+    sweeps = {}
     for prec in (gpu.F64, gpu.F32, gpu.BF16):
         x, r = A.pagerank_host(beta=0.85, tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
         assert r.converged, prec
         assert abs(x.sum() - 1.0) < 1e-12
         err = np.abs(x - xo).sum()
         assert err < 1e-10, (prec, err, r.iterations, r.iterations_f64)
+        sweeps[prec] = r.iterations
+    # Anderson-accelerated FP64: same fixed point, same stopping rule, fewer sweeps
+    x, r = A.pagerank_host(beta=0.85, tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, accel=1)
+    assert r.converged and r.residual < 1e-11
+    assert abs(x.sum() - 1.0) < 1e-12
+    assert np.abs(x - xo).sum() < 1e-10, (r.iterations, np.abs(x - xo).sum())
+    # (at scale 10 the plain iteration converges as fast: 17 sweeps both)
+    assert r.iterations <= sweeps[gpu.F64] - (2 if scale >= 14 else 0), (r.iterations, sweeps[gpu.F64])
 
 
 @pytest.mark.parametrize("scale,mode", [(14, 1), (20, -1)])
@@ -116,12 +125,12 @@ def test_relabelled_pagerank(gpu, orc, scale, mode):
     rp, ci, va, dang = rmat_csr_oracle(orc, scale, m, 3)
     xo, _, res_o = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 1e-14, 5000, threads=8)
     xo = xo / math.fsum(xo)
-    for prec in (gpu.F64, gpu.BF16):
-        x, r = A.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
-        xp, rp_ = P.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec)
+    for prec, acc in ((gpu.F64, 0), (gpu.BF16, 0), (gpu.F64, 1)):
+        x, r = A.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec, accel=acc)
+        xp, rp_ = P.pagerank_host(tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec, accel=acc)
         assert r.converged and rp_.converged
-        assert np.abs(x - xo).sum() < 1e-10, prec
-        assert np.abs(x - xp).sum() < 1e-10, prec
+        assert np.abs(x - xo).sum() < 1e-10, (prec, acc)
+        assert np.abs(x - xp).sum() < 1e-10, (prec, acc)
     # reference mode and a personalised node list (labels mapped inside)
     x, r = A.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
     xp, rp_ = P.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
@@ -143,3 +152,7 @@ def test_pagerank_argument_checks(gpu):
         m.pagerank_host(precision=gpu.BF16)  # no BF16 store
     with pytest.raises(gpu.TbslaError):
         m.pagerank_host(mode=gpu.PR_REFERENCE, precision=gpu.F32)
+    with pytest.raises(gpu.TbslaError):
+        m.pagerank_host(mode=gpu.PR_REFERENCE, accel=1)  # acceleration: dangling mode only
+    with pytest.raises(gpu.TbslaError):
+        m.pagerank_host(accel=2)
