@@ -427,6 +427,22 @@ def differentiation_bench(capi, scale=22):
                             n * 1e-15, 2000)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    # the same two solves with Anderson acceleration
+    xa = torch.empty_like(x)
+    gvals_a, gv_a = torch.empty_like(gvals), torch.empty_like(gv)
+    G.pagerank_teleport(v.data_ptr(), xa.data_ptr(), 0.85, 1e-15, 2000, accel=1)
+    G.pagerank_adjoint(v.data_ptr(), xa.data_ptr(), w.data_ptr(), gvals_a.data_ptr(), gv_a.data_ptr(), 0.85,
+                       n * 1e-15, 2000, accel=1)  # warm: graphs, ring buffers
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    rfa = G.pagerank_teleport(v.data_ptr(), xa.data_ptr(), 0.85, 1e-15, 2000, accel=1)
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    raa = G.pagerank_adjoint(v.data_ptr(), xa.data_ptr(), w.data_ptr(), gvals_a.data_ptr(), gv_a.data_ptr(), 0.85,
+                             n * 1e-15, 2000, accel=1)
+    torch.cuda.synchronize()
+    t5 = time.perf_counter()
+    accel_grad_diff = float((gvals_a - gvals).abs().max() / gvals.abs().max())
     # fourth-order differences of the GPU forward on 16 random edges
     _, _, vals = G.csr_download()
     base = torch.from_numpy(vals).to(dev)
@@ -455,6 +471,9 @@ def differentiation_bench(capi, scale=22):
         "graph": f"R-MAT scale {scale}, 2^{scale + 4} draws, seed 1", "edges": nnz,
         "forward_ms": round((t1 - t0) * 1e3, 2), "forward_sweeps": rf.iterations,
         "adjoint_ms": round((t2 - t1) * 1e3, 2), "adjoint_sweeps": ra.iterations,
+        "anderson": {"forward_ms": round((t4 - t3) * 1e3, 2), "forward_sweeps": rfa.iterations,
+                     "adjoint_ms": round((t5 - t4) * 1e3, 2), "adjoint_sweeps": raa.iterations,
+                     "values_gradient_max_rel_diff_to_plain": accel_grad_diff},
         "fd_edges": 16, "fd_rel_err_max": float(max(errs)), "fd_rel_err_median": float(np.median(errs))}
     G.close()
     torch.cuda.empty_cache()

@@ -335,12 +335,13 @@ typedef struct {
                          vectors, corrected by FP64 residual refinement
                          (TBSLA_PR_DANGLING only; needs TBSLA_STORE_F64 too) */
   int check_every;    /* sweeps per convergence check (0: library default) */
-  int accel;          /* TBSLA_PR_DANGLING in FP64: 0 power iteration; 1
-                         Anderson acceleration over the last two differences
-                         (the next sweep starts from the combination of the
-                         last three sweep outputs whose residual combination
-                         is smallest in the 2-norm); same stopping rule,
-                         same fixed point, fewer sweeps */
+  int accel;          /* FP64 dangling and teleport modes, and the adjoint:
+                         0 power iteration; 1 Anderson acceleration over
+                         the last two differences (the next sweep starts
+                         from the combination of the last three sweep
+                         outputs whose residual combination is smallest in
+                         the 2-norm); same stopping rule, same fixed point,
+                         fewer sweeps */
 } tbsla_pagerank_params_t;
 
 typedef struct {

@@ -365,15 +365,15 @@ class DeviceMatrix:
     def set_values(self, dtype: int, d_values: int, stream=None):
         check(lib().tbsla_matrix_set_values(self.h, dtype, d_values, stream))
 
-    def pagerank_teleport(self, d_v: int, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, stream=None):
-        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0)
+    def pagerank_teleport(self, d_v: int, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, stream=None, accel=0):
+        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0, accel)
         r = PageRankResult()
         check(lib().tbsla_pagerank_teleport(self.h, C.byref(p), d_v, d_out, C.byref(r), stream))
         return r
 
     def pagerank_adjoint(self, d_v, d_x: int, d_w: int, d_grad_values, d_grad_v, beta=0.85, tol=1e-12,
-                         max_iter=10000, stream=None):
-        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0)
+                         max_iter=10000, stream=None, accel=0):
+        p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, F64, 0, accel)
         r = PageRankResult()
         check(lib().tbsla_pagerank_adjoint(self.h, C.byref(p), d_v, d_x, d_w, d_grad_values, d_grad_v,
                                            C.byref(r), stream))

@@ -46,11 +46,12 @@ struct PrCtl {
   double inner_resid, inner_tol;
   int iter, done, converged, max_iter;
   int inner_iter, inner_done, inner_max, pad;
-  // Anderson acceleration (FP64 dangling mode): dangling mass and sum of the
-  // last three sweep outputs (slot k % 3), their residuals' Gram matrix with
-  // the newest first (gram[i][j] = r_{k-i} . r_{k-j}), and the coefficients
-  // of the next input in the newest-first outputs
-  double aa_d[3], aa_s[3];
+  // Anderson acceleration (FP64): for the last three sweep outputs (slot
+  // k % 3), the sweep term each would give as the next input (linear in it),
+  // their residuals' Gram matrix with the newest first (gram[i][j] =
+  // r_{k-i} . r_{k-j}), and the coefficients of the next input in the
+  // newest-first outputs
+  double aa_add[3];
   double gram[3][3];
   double coef[3];
   int aa_m, aa_pad;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(256) pr_normalize_kernel(double *__restrict__ 
 __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restrict__ partials, int nparts,
                                                           PrCtl *ctl, int stage) {
   const bool inner = stage == 3;
-  if ((stage <= 3 || stage == 8 || stage == 10 || stage == 12 || stage == 13) &&
+  if ((stage <= 3 || stage == 8 || stage == 10 || stage >= 12) &&
       (inner ? *(volatile int *)&ctl->inner_done : *(volatile int *)&ctl->done))
     return;
   __shared__ double sh[3][256];
@@ -308,11 +309,16 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
   case 11:  // initial adjoint vector: b = v . lambda0
     ctl->add = ctl->beta * b;
     break;
-  case 12: {  // accelerated sweep k: resid = a, dangling mass b and sum c of g_k
+  case 12:    // accelerated dangling sweep k (as stage 2)
+  case 14:    // accelerated teleport sweep k (as stage 8)
+  case 15: {  // accelerated adjoint sweep k (as stage 10)
+    // the term of the next sweep if g_k were its input, kept per slot; the
+    // Anderson step combines them like the outputs
     const int slot = ctl->iter % 3;
     ctl->resid = a;
-    ctl->aa_d[slot] = b;
-    ctl->aa_s[slot] = c;
+    ctl->aa_add[slot] = stage == 12 ? (ctl->beta * b + (1.0 - ctl->beta) * c) * ctl->inv_n
+                        : stage == 14 ? ctl->beta * b + (1.0 - ctl->beta)
+                                      : ctl->beta * b;
     ctl->d = b;
     ctl->s = c;
     ctl->iter += 1;
@@ -335,10 +341,11 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
 // The Anderson step after sweep k (one thread): with q_j = r_{k-j}, minimise
 // || q_0 - g1 (q_0 - q_1) - g2 (q_1 - q_2) ||_2 over the available history
 // (normal equations from the Gram matrix), then the next input is
-// x_{k+1} = (1 - g1) g_k + (g1 - g2) g_{k-1} + g2 g_{k-2}.  Its dangling
-// mass and sum follow from the outputs' (linear), which gives the next
-// sweep's teleport term.  Ill-conditioned systems or large coefficients fall
-// back to fewer differences, down to the plain step x_{k+1} = g_k.
+// x_{k+1} = (1 - g1) g_k + (g1 - g2) g_{k-1} + g2 g_{k-2}.  The coefficients
+// sum to 1, and the next sweep's term is affine in its input, so it is the
+// same combination of the outputs' terms.  Ill-conditioned systems or large
+// coefficients fall back to fewer differences, down to the plain step
+// x_{k+1} = g_k.
 __global__ void pr_aa_solve_kernel(PrCtl *ctl) {
   if (*(volatile int *)&ctl->done) return;
   const int k = ctl->iter - 1;        // the sweep just finished
@@ -371,10 +378,10 @@ __global__ void pr_aa_solve_kernel(PrCtl *ctl) {
   ctl->coef[2] = c2;
   ctl->aa_m = (c1 != 0.0 || c2 != 0.0) ? (c2 != 0.0 ? 2 : 1) : 0;
   const int s0 = k % 3, s1 = (k + 2) % 3, s2 = (k + 1) % 3;  // slots of g_k, g_{k-1}, g_{k-2}
-  double d = c0 * ctl->aa_d[s0], sum = c0 * ctl->aa_s[s0];
-  if (ctl->aa_m >= 1) { d += c1 * ctl->aa_d[s1]; sum += c1 * ctl->aa_s[s1]; }
-  if (ctl->aa_m >= 2) { d += c2 * ctl->aa_d[s2]; sum += c2 * ctl->aa_s[s2]; }
-  ctl->add = (ctl->beta * d + (1.0 - ctl->beta) * sum) * ctl->inv_n;
+  double add = c0 * ctl->aa_add[s0];
+  if (ctl->aa_m >= 1) add += c1 * ctl->aa_add[s1];
+  if (ctl->aa_m >= 2) add += c2 * ctl->aa_add[s2];
+  ctl->add = add;
 }
 
 // r_k = g_k - x_k into its slot, and the partial dots of r_k with r_k,
@@ -621,25 +628,41 @@ static tbsla_status_t enqueue_f64_sweep(const tbsla_matrix *A, PrWork *W, const 
     pr_normalize_kernel<<<kAffineBlocks, 256, 0, s>>>(x_out, x_in, W->n, W->ctl, W->partials);
     pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 1);
   } else {
-    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl, accel ? 12 : mode == kSweepTele ? 8 : 2);
+    pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, nparts, W->ctl,
+                                         mode == kSweepTele ? (accel ? 14 : 8) : (accel ? 12 : 2));
   }
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
 }
 
-// one accelerated iteration k (slot k % 3): g_k = G(x), residual dots, the
-// Anderson step, x <- the combination
-static tbsla_status_t enqueue_aa_iteration(const tbsla_matrix *A, PrWork *W, int k, cudaStream_t s) {
+// the ring buffers of the accelerated solves
+static tbsla_status_t pr_aa_buffers(PrWork *W) {
+  if (W->ag[0]) return TBSLA_OK;
+  for (int i = 0; i < 3; ++i) {
+    TB_TRY(pr_alloc((void **)&W->ag[i], (size_t)W->n * 8));
+    TB_TRY(pr_alloc((void **)&W->ar[i], (size_t)W->n * 8));
+  }
+  return TBSLA_OK;
+}
+
+// after sweep k wrote g_k (slot k % 3) from x: residual dots, the Anderson
+// step, x <- the combination
+static tbsla_status_t enqueue_aa_step(PrWork *W, double *x, double *partials, int k, cudaStream_t s) {
   const int s0 = k % 3, s1 = (k + 2) % 3, s2 = (k + 1) % 3;
-  double *x = W->x[0];
-  TB_TRY(enqueue_f64_sweep(A, W, x, W->ag[s0], kSweepDang, false, s, true));
   pr_aa_dots_kernel<<<kAffineBlocks, 256, 0, s>>>(W->ag[s0], x, W->ar[s0], W->ar[s1], W->ar[s2], W->n, W->ctl,
-                                                  W->partials);
-  pr_finalize_kernel<<<1, 256, 0, s>>>(W->partials, kAffineBlocks, W->ctl, 13);
+                                                  partials);
+  pr_finalize_kernel<<<1, 256, 0, s>>>(partials, kAffineBlocks, W->ctl, 13);
   pr_aa_solve_kernel<<<1, 1, 0, s>>>(W->ctl);
   pr_aa_combine_kernel<<<kAffineBlocks, 256, 0, s>>>(W->ag[s0], W->ag[s1], W->ag[s2], x, W->n, W->ctl);
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
+}
+
+// one accelerated iteration k of the forward map (dangling or teleport mode)
+static tbsla_status_t enqueue_aa_iteration(const tbsla_matrix *A, PrWork *W, int k, int mode, cudaStream_t s) {
+  double *x = W->x[0];
+  TB_TRY(enqueue_f64_sweep(A, W, x, W->ag[k % 3], mode, false, s, true));
+  return enqueue_aa_step(W, x, W->partials, k, s);
 }
 
 // one low-precision inner sweep e_in -> e_out + finalize
@@ -691,7 +714,7 @@ static tbsla_status_t get_graph(const tbsla_matrix *A, PrWork *W, int kind, int 
   for (int k = 0; k < sweeps && st == TBSLA_OK; ++k) {
     if (kind == 0) st = enqueue_f64_sweep(A, W, W->x[k & 1], W->x[(k + 1) & 1], mode, with_tmask, s);
     else if (kind == 1) st = enqueue_inner_sweep(A, W, (tbsla_dtype_t)precision, W->e[k & 1], W->e[(k + 1) & 1], s);
-    else st = enqueue_aa_iteration(A, W, k, s);
+    else st = enqueue_aa_iteration(A, W, k, mode, s);
   }
   cudaGraph_t graph = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -729,16 +752,13 @@ static tbsla_status_t run_f64(tbsla_matrix *A, PrWork *W, int mode, bool with_tm
   return TBSLA_OK;
 }
 
-// the Anderson-accelerated FP64 solve (dangling mode); result in ag[(iter-1) % 3]
-static tbsla_status_t run_aa(tbsla_matrix *A, PrWork *W, int check_every) {
-  if (!W->ag[0])
-    for (int i = 0; i < 3; ++i) {
-      TB_TRY(pr_alloc((void **)&W->ag[i], (size_t)W->n * 8));
-      TB_TRY(pr_alloc((void **)&W->ar[i], (size_t)W->n * 8));
-    }
+// the Anderson-accelerated FP64 solve (dangling or teleport mode); result in
+// ag[(iter-1) % 3]
+static tbsla_status_t run_aa(tbsla_matrix *A, PrWork *W, int mode, int check_every) {
+  TB_TRY(pr_aa_buffers(W));
   const int K = std::max(6, (check_every + 5) / 6 * 6);
   cudaGraphExec_t ex;
-  TB_TRY(get_graph(A, W, 2, K, TBSLA_F64, kSweepDang, false, &ex));
+  TB_TRY(get_graph(A, W, 2, K, TBSLA_F64, mode, false, &ex));
   while (true) {
     TB_CUDA(cudaGraphLaunch(ex, W->stream));
     TB_TRY(read_ctl(W));
@@ -769,8 +789,9 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
            "the teleport mode needs a teleport vector and FP64");
   TB_CHECK(p->precision == TBSLA_F64 || p->precision == TBSLA_F32 || p->precision == TBSLA_BF16, "bad precision");
   TB_CHECK(p->precision == TBSLA_F64 || p->mode == TBSLA_PR_DANGLING, "reduced precision needs TBSLA_PR_DANGLING");
-  TB_CHECK(p->accel == 0 || (p->accel == 1 && p->precision == TBSLA_F64 && p->mode == TBSLA_PR_DANGLING),
-           "accel = %d: Anderson acceleration (1) is for TBSLA_PR_DANGLING in FP64", p->accel);
+  TB_CHECK(p->accel == 0 || (p->accel == 1 && p->precision == TBSLA_F64 && p->mode != TBSLA_PR_REFERENCE &&
+                             nodes == nullptr),
+           "accel = %d: Anderson acceleration (1) is for the dangling and teleport modes in FP64", p->accel);
   TB_CHECK(A->values[0], "PageRank needs the F64 value store");
   TB_CHECK(p->precision == TBSLA_F64 || A->values[store_index((tbsla_dtype_t)p->precision)],
            "the requested reduced-precision value store is not present");
@@ -834,9 +855,9 @@ static tbsla_status_t pagerank_impl(tbsla_matrix *A, const tbsla_pagerank_params
   TB_CUDA(cudaGetLastError());
 
   int f64_sweeps = 0, inner_total = 0;
-  const bool accel = p->accel != 0 && p->precision == TBSLA_F64 && p->mode == TBSLA_PR_DANGLING;
+  const bool accel = p->accel != 0 && p->precision == TBSLA_F64 && p->mode != TBSLA_PR_REFERENCE;
   if (accel) {
-    if (!c.done) TB_TRY(run_aa(A, W, K));
+    if (!c.done) TB_TRY(run_aa(A, W, p->mode == TBSLA_PR_TELEPORT ? kSweepTele : kSweepDang, K));
     else TB_TRY(read_ctl(W));
     f64_sweeps = c.iter;
   } else if (p->precision == TBSLA_F64) {
@@ -959,13 +980,18 @@ static tbsla_status_t adjoint_impl(tbsla_matrix *A, const tbsla_pagerank_params_
   pr_dot_kernel<<<g, 256, 0, s>>>(W->lam[0], d_v, n, 1.0 / n, W->adj_partials);
   pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, g, W->ctl, 11);
   TB_CUDA(cudaGetLastError());
-  const int K = p->check_every > 0 ? p->check_every : 8;
+  TB_CHECK(p->accel == 0 || p->accel == 1, "accel = %d not 0 or 1", p->accel);
+  const bool accel = p->accel == 1;
+  if (accel) TB_TRY(pr_aa_buffers(W));
+  const int K = accel ? std::max(6, (p->check_every + 5) / 6 * 6) : p->check_every > 0 ? p->check_every : 8;
   int launched = 0;
   while (!c.done) {
     for (int k = 0; k < K; ++k, ++launched) {
       AdjEpi epi{};
-      epi.y = W->lam[(launched + 1) & 1];
-      epi.yold = W->lam[launched & 1];
+      // accelerated: lambda stays in lam[0] (the combination), outputs go to
+      // the ring slots; plain: ping-pong
+      epi.y = accel ? W->ag[launched % 3] : W->lam[(launched + 1) & 1];
+      epi.yold = accel ? W->lam[0] : W->lam[launched & 1];
       epi.w = d_w;
       epi.dmask = W->dmask;
       epi.v = d_v;
@@ -976,12 +1002,13 @@ static tbsla_status_t adjoint_impl(tbsla_matrix *A, const tbsla_pagerank_params_
       epi.inv_n = 1.0 / n;
       epi.n = n;
       TB_TRY(launch_product<double, double>(T, static_cast<const double *>(T->values[0]), epi.yold, epi, s));
-      pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, sweep_parts(T, true), W->ctl, 10);
+      pr_finalize_kernel<<<1, 256, 0, s>>>(W->adj_partials, sweep_parts(T, true), W->ctl, accel ? 15 : 10);
+      if (accel) TB_TRY(enqueue_aa_step(W, W->lam[0], W->adj_partials, launched, s));
     }
     TB_CUDA(cudaGetLastError());
     TB_TRY(read_ctl(W));
   }
-  const double *lam = W->lam[c.iter & 1];
+  const double *lam = accel ? (c.iter > 0 ? W->ag[(c.iter - 1) % 3] : W->lam[0]) : W->lam[c.iter & 1];
   if (d_gv) {
     // dL/dv = (beta * d . x + 1 - beta) * lambda (stage 9 leaves that factor in ctl->add)
     pr_mass_kernel<double><<<g, 256, 0, s>>>(d_x, n, W->dmask, W->adj_partials);

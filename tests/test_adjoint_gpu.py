@@ -111,8 +111,8 @@ def _rmat(gpu, orc, scale, seed):
     return A, rp, ci, va, dang
 
 
-@pytest.mark.parametrize("uniform", [True, False])
-def test_teleport_pagerank_and_adjoint_match_oracle(gpu, orc, uniform):
+@pytest.mark.parametrize("uniform,accel", [(True, 0), (False, 0), (False, 1)])
+def test_teleport_pagerank_and_adjoint_match_oracle(gpu, orc, uniform, accel):
     A, rp, ci, va, dang = _rmat(gpu, orc, 12, 4)
     n = rp.size - 1
     rng = np.random.default_rng(2)
@@ -121,7 +121,7 @@ def test_teleport_pagerank_and_adjoint_match_oracle(gpu, orc, uniform):
     dev = torch.device("cuda")
     tv, tw = torch.from_numpy(v).to(dev), torch.from_numpy(w).to(dev)
     x = torch.empty(n, dtype=torch.float64, device=dev)
-    r = A.pagerank_teleport(tv.data_ptr(), x.data_ptr(), 0.85, 1e-15, 2000)
+    r = A.pagerank_teleport(tv.data_ptr(), x.data_ptr(), 0.85, 1e-15, 2000, accel=accel)
     assert r.converged
     xo, _, _ = orc.pagerank_teleport(rp, ci, va, dang, v, 0.85, 0.0, 400)
     assert np.abs(x.cpu().numpy() - xo).sum() < 1e-13
@@ -133,7 +133,7 @@ def test_teleport_pagerank_and_adjoint_match_oracle(gpu, orc, uniform):
     gv = torch.empty(n, dtype=torch.float64, device=dev)
     # lambda is O(1) per entry: an L1 tolerance of n * 1e-15
     ra = A.pagerank_adjoint(tv.data_ptr(), x.data_ptr(), tw.data_ptr(), gvals.data_ptr(), gv.data_ptr(), 0.85,
-                            n * 1e-15, 3000)
+                            n * 1e-15, 3000, accel=accel)
     assert ra.converged
     go_vals, go_v, _ = orc.pagerank_adjoint(rp, ci, va, dang, v, xo, w, 0.85, 0.0, 400)
     assert np.max(np.abs(gvals.cpu().numpy() - go_vals)) <= 1e-10 * np.max(np.abs(go_vals))
