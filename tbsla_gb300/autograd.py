@@ -66,10 +66,12 @@ class CsrSpMV(torch.autograd.Function):
 
 class PageRankTeleport(torch.autograd.Function):
     """x* of x = beta A x + (beta d.x + 1 - beta) v; gradients by the adjoint
-    solve lambda = beta A^T lambda + beta d (v.lambda) + dL/dx*."""
+    solve lambda = beta A^T lambda + beta d (v.lambda) + dL/dx*.  Both solves
+    use Anderson acceleration unless accel = 0 (same fixed points and
+    stopping rules, several times fewer sweeps for the adjoint)."""
 
     @staticmethod
-    def forward(ctx, values, v, matrix, beta=0.85, tol=1e-14, max_iter=10000):
+    def forward(ctx, values, v, matrix, beta=0.85, tol=1e-14, max_iter=10000, accel=1):
         if values.dtype != torch.float64 or v.dtype != torch.float64:
             raise TypeError("PageRank runs in FP64")
         vals = values.detach().contiguous()
@@ -77,16 +79,16 @@ class PageRankTeleport(torch.autograd.Function):
         matrix.set_values(capi.F64, vals.data_ptr(), _stream())
         n = matrix.info().n_col
         x = torch.empty(n, dtype=torch.float64, device=v.device)
-        matrix.pagerank_teleport(vv.data_ptr(), x.data_ptr(), beta, tol, max_iter, _stream())
+        matrix.pagerank_teleport(vv.data_ptr(), x.data_ptr(), beta, tol, max_iter, _stream(), accel=accel)
         ctx.matrix = matrix
-        ctx.params = (beta, tol, max_iter, int(matrix.info().stored))
+        ctx.params = (beta, tol, max_iter, int(matrix.info().stored), accel)
         ctx.save_for_backward(vv, x)
         return x
 
     @staticmethod
     def backward(ctx, gx):
         vv, x = ctx.saved_tensors
-        beta, tol, max_iter, nnz = ctx.params
+        beta, tol, max_iter, nnz, accel = ctx.params
         gx = gx.contiguous()
         gvals = torch.empty(nnz, dtype=torch.float64, device=x.device) if ctx.needs_input_grad[0] else None
         gv = torch.empty_like(x) if ctx.needs_input_grad[1] else None
@@ -94,8 +96,9 @@ class PageRankTeleport(torch.autograd.Function):
         adj_tol = max(tol, 1e-15) * x.numel()
         ctx.matrix.pagerank_adjoint(vv.data_ptr(), x.data_ptr(), gx.data_ptr(),
                                     None if gvals is None else gvals.data_ptr(),
-                                    None if gv is None else gv.data_ptr(), beta, adj_tol, max_iter, _stream())
-        return gvals, gv, None, None, None, None
+                                    None if gv is None else gv.data_ptr(), beta, adj_tol, max_iter, _stream(),
+                                    accel=accel)
+        return gvals, gv, None, None, None, None, None
 
 
 def csr_spmv(matrix, values: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
@@ -103,5 +106,5 @@ def csr_spmv(matrix, values: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
 
 
 def pagerank(matrix, values: torch.Tensor, v: torch.Tensor, beta: float = 0.85, tol: float = 1e-14,
-             max_iter: int = 10000) -> torch.Tensor:
-    return PageRankTeleport.apply(values, v, matrix, beta, tol, max_iter)
+             max_iter: int = 10000, accel: int = 1) -> torch.Tensor:
+    return PageRankTeleport.apply(values, v, matrix, beta, tol, max_iter, accel)

@@ -209,3 +209,5 @@ def test_autograd_shim_gradcheck(gpu, orc):
     wt = torch.from_numpy(np.random.default_rng(1).standard_normal(n)).to(dev)
     f = lambda a, b: (ag.pagerank(P, a, b, tol=1e-15) * wt).sum()
     assert torch.autograd.gradcheck(f, (pv, tv), eps=1e-7, atol=1e-7, rtol=1e-5)
+    f0 = lambda a, b: (ag.pagerank(P, a, b, tol=1e-15, accel=0) * wt).sum()
+    assert torch.autograd.gradcheck(f0, (pv, tv), eps=1e-7, atol=1e-7, rtol=1e-5)
