@@ -397,6 +397,47 @@ def batching_bench(capi, ppr_scale=22):
     out["ppr_256"] = res
     G.close()
     torch.cuda.empty_cache()
+    # ---- k vectors through one CSR matrix (tbsla_spmm) vs k products, cqmat 2^22
+    N = 1 << 22
+    A = capi.DeviceMatrix.generate("CSR", "cqmat", N, N, C_HEADLINE, Q_HEADLINE, 0,
+                                   stores=capi.STORE_F64 | capi.STORE_F32)
+    st = int(A.info().stored)
+    s = torch.cuda.current_stream().cuda_stream
+    sp = {}
+    for store, tdt, vb in ((capi.F64, torch.float64, 8), (capi.F32, torch.float32, 4)):
+        for k in (8, 32):
+            X = torch.rand((N, k), dtype=tdt, device=dev)
+            Y = torch.empty((N, k), dtype=tdt, device=dev)
+            xs = [torch.rand(N, dtype=tdt, device=dev) for _ in range(k)]
+            y1 = torch.empty(N, dtype=tdt, device=dev)
+
+            def singles():
+                for xv in xs:
+                    A.spmv_ex(store, store, xv.data_ptr(), store, y1.data_ptr(), 0, s)
+            A.spmm(store, k, X.data_ptr(), k, Y.data_ptr(), k, s)
+            singles()
+            e0, e1 = _events()
+            e0.record()
+            for _ in range(5):
+                A.spmm(store, k, X.data_ptr(), k, Y.data_ptr(), k, s)
+            e1.record()
+            torch.cuda.synchronize()
+            mm_ms = e0.elapsed_time(e1) / 5
+            e0.record()
+            for _ in range(5):
+                singles()
+            e1.record()
+            torch.cuda.synchronize()
+            single_ms = e0.elapsed_time(e1) / 5
+            algo = st * (vb + 4) + (N + 1) * 4 + 2 * N * k * vb
+            sp[f"{'f64' if store == capi.F64 else 'f32'}_k{k}"] = {
+                "spmm_ms": round(mm_ms, 4), "spmm_GB_s": round(algo / mm_ms / 1e6, 1),
+                "fma_per_s_T": round(st * k / mm_ms / 1e9, 3),
+                "k_products_ms": round(single_ms, 4), "speedup": round(single_ms / mm_ms, 2)}
+            del X, Y, xs
+    out["csr_spmm_cqmat_2^22"] = sp
+    A.close()
+    torch.cuda.empty_cache()
     return out
 
 

@@ -237,6 +237,18 @@ tbsla_status_t tbsla_matrix_set_values(tbsla_matrix_t *A, tbsla_dtype_t type, co
 tbsla_status_t tbsla_dense_spmm(const tbsla_matrix_t *A, tbsla_dtype_t store, int k, const void *d_X,
                                 int64_t ldx, void *d_Y, int64_t ldy, void *stream);
 
+/* Y = A X for k vectors of a CSR or COO / SCOO handle, X and Y row-major
+ * (vector index fastest: X[j*ldx + c] is entry j of vector c, ldx, ldy >= k;
+ * X has x_extent rows, Y n_row rows).  FP64 vectors for the F64 store, FP32
+ * for F32 and BF16.  Vectors go in panels of up to 32, a group of lanes per
+ * row with lane c on vector c: one gather brings a row of X for the panel,
+ * and the matrix is streamed once per panel.  Column c equals the one-vector
+ * product of vector c summed in stored order (bit for bit for rows of at most
+ * 32 entries with TBSLA_TUNE_SHORT_ROWS = 0).  No reference counterpart (the
+ * reference multiplies one vector at a time). */
+tbsla_status_t tbsla_spmm(const tbsla_matrix_t *A, tbsla_dtype_t store, int k, const void *d_X, int64_t ldx,
+                          void *d_Y, int64_t ldy, void *stream);
+
 /* r = A (A x + x): Matrix::a_axpx_ (Matrix.cpp:6-11), square matrices; the
  * "+ x" is fused into the first product.  d_tmp: n_row doubles of device
  * scratch (required: the call is stream-ordered and holds no handle lock). */

@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
         "tbsla_ell_download": ([P, _vp, _vp], st),
         "tbsla_dense_download": ([P, _vp], st),
         "tbsla_dense_spmm": ([P, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp], st),
+        "tbsla_spmm": ([P, C.c_int, C.c_int, _vp, C.c_int64, _vp, C.c_int64, _vp], st),
         "tbsla_autotune_batch": ([_vp, C.POINTER(AutotuneResult)], st),
         "tbsla_autotune_ppr": ([P, C.c_int, C.c_int, C.POINTER(AutotuneResult)], st),
     }
@@ -413,6 +414,10 @@ class DeviceMatrix:
 
     def dense_spmm(self, store: int, k: int, d_X: int, ldx: int, d_Y: int, ldy: int, stream=None):
         check(lib().tbsla_dense_spmm(self.h, store, k, d_X, ldx, d_Y, ldy, stream))
+
+    def spmm(self, store: int, k: int, d_X: int, ldx: int, d_Y: int, ldy: int, stream=None):
+        """Y = A X for k row-major vectors (CSR, COO, SCOO)."""
+        check(lib().tbsla_spmm(self.h, store, k, d_X, ldx, d_Y, ldy, stream))
 
     def to_csr(self, stores=STORE_F64):
         """CSR handle converted on the device from this COO / SCOO handle."""
