@@ -4,8 +4,9 @@ Headline (``value``): CSR FP64 SpMV y = A x on the cqmat matrix n = 2^24, c = 16
 q = 0.1, seed 0 (268,435,336 stored entries, 3.56 GB of algorithmic traffic per
 product), in GB/s of algorithmic bytes over device time with the matrix and x
 resident in HBM.  Every section runs with 32-byte L2 fetches
-(tbsla_set_l2_fetch_granularity); the headline keeps x evict-last in a 64 MiB
-persisting L2 set-aside (tbsla_set_l2_persisting).  A "step" is one product.  ``e2e`` is the same metric through
+(tbsla_set_l2_fetch_granularity); the headline and the format sweep keep x
+evict-last in a 64 MiB persisting L2 set-aside (tbsla_set_l2_persisting), the
+other sections run with the context's set-aside.  A "step" is one product.  ``e2e`` is the same metric through
 the C ABI's host-vector call (tbsla_spmv_host) on pinned host vectors: x is
 copied into HBM and the product writes y into host memory over NVLink-C2C,
 both inside the timed region.
@@ -206,9 +207,17 @@ def time_product(capi, A, store, vt, n_row, n_col, reps=10):
 
 
 def format_sweep(capi, peak, log2n=24):
-    """Every format / store of the configuration, device GB/s."""
+    """Every format / store of the configuration, device GB/s.  As the
+    headline: a 64 MiB persisting L2 set-aside (restored after) with x loaded
+    evict-last (ELL: 30 % of x, its best)."""
     import torch
-    out = {}
+    L = capi.lib()
+    sa0, sa_max = C.c_size_t(), C.c_size_t()
+    capi.check(L.tbsla_get_l2_persisting(C.byref(sa0), C.byref(sa_max)))
+    capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
+    sa_set = C.c_size_t()
+    capi.check(L.tbsla_get_l2_persisting(C.byref(sa_set), None))
+    out = {"l2": {"persisting_bytes": int(sa_set.value), "x_evict_last_fraction": "1.0 (ELL 0.3)"}}
     n = 1 << log2n
     nd = 32768 if log2n >= 24 else 8192  # DENSE order (small cases stay a few GB)
     cases = [("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
@@ -220,6 +229,8 @@ def format_sweep(capi, peak, log2n=24):
              (f"CSR_f64_cdiag_2^{log2n + 2}", "CSR", "cdiag", 4 * n, 1, 1, capi.F64, capi.F64)]
     for (key, fmt, gen, nn, c, stores, store, vt) in cases:
         A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
+        if fmt != "ELL":
+            A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_HEADLINE)
         i = A.info()
         ms = time_product(capi, A, store, vt, i.n_row, i.n_col)
         vb = {capi.F64: 8, capi.F32: 4, capi.BF16: 2}[store]
@@ -238,6 +249,7 @@ def format_sweep(capi, peak, log2n=24):
         A.close()
         torch.cuda.empty_cache()
     out[f"DENSE_multi_vector_{nd}_k64"] = dense_multi(capi, nd, 64)
+    capi.check(L.tbsla_set_l2_persisting(sa0.value))
     return out
 
 
