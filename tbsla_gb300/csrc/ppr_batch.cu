@@ -13,8 +13,13 @@
 //   x_c <- beta A x_c + (beta d.x_c + 1 - beta) v_c,
 // stopped on its own when ||x_c - x_c,prev||_1 < tol (or max_iter sweeps);
 // a stopped vector is frozen (its lanes copy the old value), and a tile
-// whose vectors have all stopped skips its kernels.  All sums have a fixed
-// order: results do not depend on scheduling.
+// whose vectors have all stopped skips its kernels.  Every check_every
+// sweeps the host writes out the vectors that stopped and, when the ones
+// still running fit in fewer tiles, repacks them (iterates, seeds, control
+// state) so that no tile sweeps for one slow vector while its other lanes
+// idle.  A column's arithmetic and its reduction order do not depend on its
+// tile or lane, so repacking leaves every result bit for bit as it was.
+// All sums have a fixed order: results do not depend on scheduling.
 //
 // Large skewed graphs run on the degree-relabelled copy (pr_relabel.cu);
 // seeds are mapped in and the results gathered back to the original labels.
@@ -209,15 +214,34 @@ __global__ void ppr_dangling_kernel(const int *__restrict__ colidx, const T *__r
     if (values[k] != T(0)) dmask[colidx[k]] = 0;
 }
 
-// out[c*n + v] = tile(c)[map(v)][c % KT] as FP64
+// out[v_j * n + u] = column c_j of a tile at row map(u), as FP64, for the
+// cnt (column, vector) pairs of a list
+struct PprPicks {
+  int cnt;
+  int col[32], vec[32];
+};
 template <typename T, int KT>
-__global__ void ppr_gather_kernel(const T *__restrict__ x, int n, const int *__restrict__ newid, int k_in_tile,
-                                  int col0, double *__restrict__ out) {
-  const int64_t total = (int64_t)n * k_in_tile;
+__global__ void ppr_pick_kernel(const T *__restrict__ x, int n, const int *__restrict__ newid, PprPicks pk,
+                                double *__restrict__ out) {
+  const int64_t total = (int64_t)n * pk.cnt;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(t / n), v = (int)(t % n);
-    const int i = newid ? newid[v] : v;
-    out[(size_t)(col0 + c) * n + v] = (double)x[(size_t)i * KT + c];
+    const int j = (int)(t / n), u = (int)(t % n);
+    const int i = newid ? newid[u] : u;
+    out[(size_t)pk.vec[j] * n + u] = (double)x[(size_t)i * KT + pk.col[j]];
+  }
+}
+
+// repacked layout: slot s of the new tiles takes old slot map[s] (-1: zero)
+template <typename T, int KT>
+__global__ void ppr_move_kernel(const T *__restrict__ src, T *__restrict__ dst, int n, const int *__restrict__ map,
+                                int new_tiles) {
+  const int64_t total = (int64_t)new_tiles * n * KT;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(q % KT);
+    const int64_t ti = q / KT;
+    const int i = (int)(ti % n), t = (int)(ti / n);
+    const int from = map[t * KT + c];
+    dst[q] = from < 0 ? T(0) : src[((size_t)(from / KT) * n + i) * KT + (from % KT)];
   }
 }
 
@@ -251,10 +275,11 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   // seeds: bit c of seeds[t*n + i] = row i is a seed of vector t*KT + c
   std::vector<unsigned> seeds((size_t)tiles * n, 0u);
   std::vector<double> inv((size_t)tiles * KT, 0.0);
+  std::vector<std::vector<int>> seed_sets((size_t)k);  // per vector, in the matrix's labels
   for (int c = 0; c < k; ++c) {
     const int b = offsets[c], e = offsets[c + 1];
     TB_CHECK(e > b, "vector %d has an empty seed set", c);
-    std::vector<int> dist;
+    std::vector<int> &dist = seed_sets[(size_t)c];
     for (int q = b; q < e; ++q) {
       int v = nodes[q];
       TB_CHECK(v >= 0 && v < n, "seed %d of vector %d outside [0, %d)", v, c, n);
@@ -337,18 +362,29 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
                                              p->max_iter, std::min(KT, k - t * KT), 1);
   }
   if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank init"); }
-  // sweeps: each round runs K sweeps on every tile (stopped tiles return at once)
+  // Sweeps in rounds of K on every tile of the current layout (stopped tiles
+  // return at once).  After each round the vectors that stopped are written
+  // out and dropped; when the live vectors fit in fewer tiles they are
+  // repacked (compaction), so a tile never keeps sweeping for one slow
+  // vector while its other lanes idle.  All tiles of a layout sweep in step:
+  // the layout's iterates start in x[base] and sweep j reads x[(base+j)&1].
   const int K = p->check_every > 0 ? p->check_every : 8;
-  std::vector<TileCtl> hdone((size_t)tiles);
-  int rounds = 0;
+  int cur_tiles = tiles, base = 0;
+  std::vector<int> slot_vec((size_t)tiles * KT, -1);  // vector in each slot, -1 for none
+  for (int c = 0; c < k; ++c) slot_vec[(size_t)c] = c;
+  std::vector<TileCtl> htc((size_t)tiles);
+  std::vector<ColCtl> hcc((size_t)tiles * KT);
+  int *d_map = nullptr;
+  alloc((void **)&d_map, (size_t)tiles * KT * sizeof(int));
+  if (st != TBSLA_OK) { cleanup(); return st; }
+  std::vector<char> tile_live((size_t)tiles, 1);
+  int phase = 0;
   while (true) {
-    for (int k2 = 0; k2 < K; ++k2) {
-      const int sweep = rounds * K + k2;
-      for (int t = 0; t < tiles; ++t) {
-        // tile t runs its sweeps in step with the others until it stops, so
-        // the parity of `sweep` is the parity of its own sweep count
-        const T *xo = x[sweep & 1] + (size_t)t * n * KT;
-        T *xn = x[(sweep + 1) & 1] + (size_t)t * n * KT;
+    for (int k2 = 0; k2 < K; ++k2, ++phase) {
+      for (int t = 0; t < cur_tiles; ++t) {
+        if (!tile_live[(size_t)t]) continue;  // stopped in an earlier round
+        const T *xo = x[(base + phase) & 1] + (size_t)t * n * KT;
+        T *xn = x[(base + phase + 1) & 1] + (size_t)t * n * KT;
         double *pt = partials + (size_t)t * nparts * KT * 2;
         const unsigned *sd = d_seeds + (size_t)t * n;
         const ColCtl *cl = d_col + (size_t)t * KT;
@@ -358,36 +394,91 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
         if (n_crow)
           ppr_fixup_kernel<T, KT><<<grid_fx, 256, 0, s>>>(d_crow, n_crow, chunk, xo, xn, sd, dmask, cl, iv, beta,
                                                           pt, grid_mm, d_tile + t);
-        ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm,
-                                                 d_col + (size_t)t * KT, d_tile + t, beta, p->tol, p->max_iter,
-                                                 std::min(KT, k - t * KT), 0);
+        ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm, d_col + (size_t)t * KT,
+                                                 d_tile + t, beta, p->tol, p->max_iter, KT, 0);
       }
     }
-    ++rounds;
-    if (cudaMemcpyAsync(hdone.data(), d_tile, hdone.size() * sizeof(TileCtl), cudaMemcpyDeviceToHost, s) !=
+    if (cudaMemcpyAsync(htc.data(), d_tile, (size_t)cur_tiles * sizeof(TileCtl), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(hcc.data(), d_col, (size_t)cur_tiles * KT * sizeof(ColCtl), cudaMemcpyDeviceToHost, s) !=
             cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
       cleanup();
       return fail(TBSLA_ERR_CUDA, "batched PageRank sweeps failed");
     }
-    bool all = true;
-    for (auto &tc : hdone) all = all && tc.done;
-    if (all) break;
+    // write out and drop the vectors that stopped (a stopped vector is
+    // frozen: its tile's last iterate, x[(base + tile iter) & 1], holds it;
+    // a stopped tile's vectors have all stopped, or max_iter is 0)
+    int live = 0, busy = 0;
+    for (int t = 0; t < cur_tiles; ++t) {
+      PprPicks pk;
+      pk.cnt = 0;
+      for (int c = 0; c < KT; ++c) {
+        const int v = slot_vec[(size_t)t * KT + c];
+        if (v < 0) continue;
+        const ColCtl &cc = hcc[(size_t)t * KT + c];
+        if (cc.done || htc[(size_t)t].done) {
+          pk.col[pk.cnt] = c;
+          pk.vec[pk.cnt++] = v;
+          if (iters_out) iters_out[v] = cc.iter;
+          if (resid_out) resid_out[v] = cc.resid;
+          slot_vec[(size_t)t * KT + c] = -1;
+        } else {
+          ++live;
+        }
+      }
+      if (pk.cnt) {
+        const T *xf = x[(base + htc[(size_t)t].iter) & 1] + (size_t)t * n * KT;
+        ppr_pick_kernel<T, KT><<<152 * 8, 256, 0, s>>>(xf, n, newid_dev, pk, d_out);
+      }
+      tile_live[(size_t)t] = !htc[(size_t)t].done;
+      busy += !htc[(size_t)t].done;
+    }
+    if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank results"); }
+    if (live == 0) break;
+    const int need = (live + KT - 1) / KT;
+    if (need < busy) {
+      // repack the live vectors into `need` tiles: their iterates (all in
+      // x[(base+phase)&1], every live tile having run all `phase` sweeps)
+      // move to the other buffer, which becomes the new layout's start
+      std::vector<int> map((size_t)need * KT, -1), nvec((size_t)need * KT, -1);
+      std::vector<unsigned> nseeds((size_t)need * n, 0u);
+      std::vector<double> ninv((size_t)need * KT, 0.0);
+      std::vector<ColCtl> ncol((size_t)need * KT);
+      int q = 0;
+      for (int t = 0; t < cur_tiles; ++t)
+        for (int c = 0; c < KT; ++c) {
+          const int v = slot_vec[(size_t)t * KT + c];
+          if (v < 0) continue;
+          map[(size_t)q] = t * KT + c;
+          nvec[(size_t)q] = v;
+          ncol[(size_t)q] = hcc[(size_t)t * KT + c];
+          ninv[(size_t)q] = inv[(size_t)t * KT + c];
+          for (int u : seed_sets[(size_t)v]) nseeds[(size_t)(q / KT) * n + u] |= 1u << (q % KT);
+          ++q;
+        }
+      for (size_t r = (size_t)q; r < ncol.size(); ++r) ncol[r] = ColCtl{0.0, 0.0, 0, 1};
+      std::vector<TileCtl> ntile((size_t)need, TileCtl{0, 0, {0, 0}});
+      up(d_map, map.data(), map.size() * sizeof(int));
+      up(d_seeds, nseeds.data(), nseeds.size() * sizeof(unsigned));
+      up(d_inv, ninv.data(), ninv.size() * sizeof(double));
+      up(d_col, ncol.data(), ncol.size() * sizeof(ColCtl));
+      up(d_tile, ntile.data(), ntile.size() * sizeof(TileCtl));
+      if (e != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack: %s", cudaGetErrorString(e)); }
+      const int src = (base + phase) & 1;
+      ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(x[src], x[src ^ 1], n, d_map, need);
+      if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack"); }
+      base = src ^ 1;
+      phase = 0;
+      cur_tiles = need;
+      slot_vec = nvec;
+      inv = ninv;
+      std::fill(tile_live.begin(), tile_live.end(), 1);
+    }
   }
-  // results: tile t's last iterate is in x[iter_t % 2]
-  for (int t = 0; t < tiles; ++t) {
-    const T *xf = x[hdone[(size_t)t].iter & 1] + (size_t)t * n * KT;
-    ppr_gather_kernel<T, KT><<<152 * 8, 256, 0, s>>>(xf, n, newid_dev, std::min(KT, k - t * KT), t * KT, d_out);
-  }
-  std::vector<ColCtl> fin((size_t)tiles * KT);
-  if (cudaMemcpyAsync(fin.data(), d_col, fin.size() * sizeof(ColCtl), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess) {
+  if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     cleanup();
     return fail(TBSLA_ERR_CUDA, "batched PageRank results");
-  }
-  for (int c = 0; c < k; ++c) {
-    if (iters_out) iters_out[c] = fin[(size_t)c].iter;
-    if (resid_out) resid_out[c] = fin[(size_t)c].resid;
   }
   cleanup();
   return TBSLA_OK;

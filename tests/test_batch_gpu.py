@@ -104,6 +104,44 @@ def test_batched_ppr_matches_oracle(gpu, orc, tile, relabel):
     assert np.max(np.abs(got32 - got).sum(axis=1)) < 1e-5
 
 
+@pytest.mark.parametrize("tile,check_every,prec", [(8, 1, "F64"), (4, 3, "F64"), (32, 2, "F32")])
+def test_batched_ppr_repacking_is_exact(gpu, tile, check_every, prec):
+    """Vectors stop at different sweeps and the running ones are repacked
+    into fewer tiles between rounds; a column's arithmetic does not depend
+    on its tile or lane, so each vector equals the same vector solved alone
+    bit for bit, with the same sweep count and residual."""
+    scale = 11
+    A = gpu.DeviceMatrix.rmat_pagerank(scale, 16 << scale, seed=9, stores=gpu.STORE_F64 | gpu.STORE_F32)
+    n = A.info().n_row
+    rng = np.random.default_rng(3)
+    k = 37
+    sets = _seed_sets(rng, n, k)
+    dev = torch.device("cuda")
+    precision = getattr(gpu, prec)
+    tol = 1e-12 if prec == "F64" else 1e-6
+    out = torch.empty(k * n, dtype=torch.float64, device=dev)
+    its, res = gpu.ppr_batched(A, sets, out.data_ptr(), tol=tol, max_iter=1000, tile=tile, precision=precision,
+                               check_every=check_every)
+    assert its.min() < its.max()  # the vectors stop at different sweeps
+    got = out.view(k, n)
+    one = torch.empty(n, dtype=torch.float64, device=dev)
+    for c in (0, 5, int(np.argmin(its)), int(np.argmax(its)), k - 1):
+        i1, r1 = gpu.ppr_batched(A, [sets[c]], one.data_ptr(), tol=tol, max_iter=1000, tile=tile,
+                                 precision=precision, check_every=check_every)
+        assert torch.equal(one, got[c]), c
+        assert int(i1[0]) == int(its[c]) and float(r1[0]) == float(res[c])
+    # a sweep cap stops every vector at max_iter; max_iter 0 returns the start vectors
+    its5, _ = gpu.ppr_batched(A, sets, out.data_ptr(), tol=0.0, max_iter=5, tile=tile, precision=precision,
+                              check_every=check_every)
+    assert (its5 == 5).all()
+    its0, _ = gpu.ppr_batched(A, sets[:3], out.data_ptr(), tol=tol, max_iter=0, tile=tile)
+    assert (its0 == 0).all()
+    v = np.zeros(n)
+    seeds = np.unique(sets[1])
+    v[seeds] = 1.0 / seeds.size
+    assert np.array_equal(out.view(k, n)[1].cpu().numpy(), v)
+
+
 def test_autotuners_keep_results(gpu, orc):
     """The tuners time candidates and keep the fastest; products and
     PageRank vectors are the same before and after."""
