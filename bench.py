@@ -12,7 +12,8 @@ copied into HBM and the product writes y into host memory over NVLink-C2C,
 both inside the timed region.
 
 Also reported (single-GPU runs): the format sweep of the same configuration
-(ELL/COO/SCOO FP64, CSR FP32/BF16 stores, DENSE n = 32768, cdiag n = 2^26) and
+(CSR/ELL/COO/SCOO FP64 SpMV and a_axpx_, CSR FP32/BF16 stores, DENSE n = 32768,
+cdiag n = 2^26) and
 PageRank on the R-MAT graph 2^24 nodes / 2^28 edge draws, (a,b,c,d) = (0.57,
 0.19, 0.19, 0.05), seed 1, damping 0.85, dangling mass redistributed, stopped at
 L1 residual 1e-10: time to tolerance in FP64 and with FP32 / BF16 stored values
@@ -211,6 +212,25 @@ def time_product(capi, A, store, vt, n_row, n_col, reps=10):
     return e0.elapsed_time(e1) / reps
 
 
+def time_axpx(capi, A, n, reps=10):
+    """Device time of one a_axpx_ (r = A (A x + x), tbsla_a_axpx, FP64)."""
+    import torch
+    x = torch.rand(n, dtype=torch.float64, device="cuda")
+    r = torch.empty(n, dtype=torch.float64, device="cuda")
+    tmp = torch.empty(n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        A.a_axpx(x.data_ptr(), r.data_ptr(), tmp.data_ptr(), 0, s.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        A.a_axpx(x.data_ptr(), r.data_ptr(), tmp.data_ptr(), 0, s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def format_sweep(capi, peak, log2n=24):
     """Every format / store of the configuration, device GB/s.  As the
     headline: a 64 MiB persisting L2 set-aside (restored after) with x loaded
@@ -225,7 +245,8 @@ def format_sweep(capi, peak, log2n=24):
     out = {"l2": {"persisting_bytes": int(sa_set.value), "x_evict_last": f"first {X_KEEP_HEADLINE:.0%} of x's addresses (ELL: 30 % of its loads)"}}
     n = 1 << log2n
     nd = 32768 if log2n >= 24 else 8192  # DENSE order (small cases stay a few GB)
-    cases = [("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
+    cases = [("CSR_f64", "CSR", "cqmat", n, 16, 1, capi.F64, capi.F64),
+             ("CSR_f32", "CSR", "cqmat", n, 16, 2, capi.F32, capi.F32),
              ("CSR_bf16", "CSR", "cqmat", n, 16, 4, capi.BF16, capi.F32),
              ("ELL_f64", "ELL", "cqmat", n, 16, 1, capi.F64, capi.F64),
              ("COO_f64", "COO", "cqmat", n, 16, 1, capi.F64, capi.F64),
@@ -252,6 +273,13 @@ def format_sweep(capi, peak, log2n=24):
         gbs = algo / (ms * 1e-3) / 1e9
         out[key] = {"ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_hbm": round(gbs / peak, 3),
                     "stored": int(i.stored), "gflops": round(2 * i.stored / (ms * 1e-3) / 1e9, 1)}
+        if gen == "cqmat" and fmt in ("CSR", "ELL", "COO", "SCOO") and store == capi.F64:
+            # a_axpx_ (Matrix.cpp:6-11): two products and the "+ x" (fused
+            # into the first product's epilogue); bytes 2 x the matrix + 5 n-vectors
+            ax_ms = time_axpx(capi, A, nn)
+            ax = 2 * (algo - 2 * nn * xb) + 5 * nn * 8
+            out[key]["a_axpx"] = {"ms": round(ax_ms, 4), "GB_s": round(ax / (ax_ms * 1e-3) / 1e9, 1),
+                                  "frac_hbm": round(ax / (ax_ms * 1e-3) / 1e9 / peak, 3)}
         A.close()
         torch.cuda.empty_cache()
     out[f"DENSE_multi_vector_{nd}_k64"] = dense_multi(capi, nd, 64)
