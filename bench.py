@@ -48,12 +48,13 @@ C_HEADLINE = 16
 Q_HEADLINE = 0.1
 L2_FETCH_BYTES = 32  # L2 fetch granularity of the whole run (tbsla_set_l2_fetch_granularity)
 L2_PERSIST_BYTES = 64 << 20  # persisting L2 set-aside of the headline (tbsla_set_l2_persisting)
-# the headline and the format sweep load the first 45 % of x's addresses
-# evict-last (range policy: TBSLA_TUNE_X_L2_KEEP 0.45 with TBSLA_TUNE_X_L2_RANGE
-# 1; FP64 x: 60 MB, inside the 67.8 MB set-aside, the same lines every
-# product); ELL keeps 30 % of its loads evict-last (fractional), its best
+# the headline and the format sweep load as much of x evict-last as the
+# 67.8 MB set-aside holds, the same lines every product (range policy:
+# TBSLA_TUNE_X_L2_KEEP with TBSLA_TUNE_X_L2_RANGE 1): the first 45 % of an
+# FP64 x of 2^24 entries (60 MB), all of an FP32 one (64 MiB)
 X_KEEP_HEADLINE = 0.45
 X_RANGE_HEADLINE = 1
+X_KEEP_FP32 = 1.0
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
@@ -233,8 +234,9 @@ def time_axpx(capi, A, n, reps=10):
 
 def format_sweep(capi, peak, log2n=24):
     """Every format / store of the configuration, device GB/s.  As the
-    headline: a 64 MiB persisting L2 set-aside (restored after) with x loaded
-    evict-last by address (ELL: 30 % of its loads, its best)."""
+    headline: a 64 MiB persisting L2 set-aside (restored after; every case
+    starts with it cleared) holding the first addresses of x, as much as
+    fits."""
     import torch
     L = capi.lib()
     sa0, sa_max = C.c_size_t(), C.c_size_t()
@@ -242,7 +244,7 @@ def format_sweep(capi, peak, log2n=24):
     capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
     sa_set = C.c_size_t()
     capi.check(L.tbsla_get_l2_persisting(C.byref(sa_set), None))
-    out = {"l2": {"persisting_bytes": int(sa_set.value), "x_evict_last": f"first {X_KEEP_HEADLINE:.0%} of x's addresses (ELL: 30 % of its loads)"}}
+    out = {"l2": {"persisting_bytes": int(sa_set.value), "x_evict_last": f"first {X_KEEP_HEADLINE:.0%} of an FP64 x's addresses, all of an FP32 x"}}
     n = 1 << log2n
     nd = 32768 if log2n >= 24 else 8192  # DENSE order (small cases stay a few GB)
     cases = [("CSR_f64", "CSR", "cqmat", n, 16, 1, capi.F64, capi.F64),
@@ -254,10 +256,11 @@ def format_sweep(capi, peak, log2n=24):
              (f"DENSE_f64_{nd}", "DENSE", "cqmat", nd, 16, 1, capi.F64, capi.F64),
              (f"CSR_f64_cdiag_2^{log2n + 2}", "CSR", "cdiag", 4 * n, 1, 1, capi.F64, capi.F64)]
     for (key, fmt, gen, nn, c, stores, store, vt) in cases:
+        # a cleared set-aside: no persisting lines of the previous case's x
+        capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
         A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
-        if fmt != "ELL":
-            A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_HEADLINE)
-            A.tune(capi.TUNE_X_L2_RANGE, X_RANGE_HEADLINE)
+        A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_HEADLINE if vt == capi.F64 else X_KEEP_FP32)
+        A.tune(capi.TUNE_X_L2_RANGE, X_RANGE_HEADLINE)
         i = A.info()
         ms = time_product(capi, A, store, vt, i.n_row, i.n_col)
         vb = {capi.F64: 8, capi.F32: 4, capi.BF16: 2}[store]

@@ -140,8 +140,11 @@ tbsla_status_t tbsla_dense_create(int n_row, int n_col, int ln_row, int ln_col,
 
 tbsla_status_t tbsla_matrix_destroy(tbsla_matrix_t *A);
 /* Kernel choice for a format with several (CSR: 0 = direct row bins, the
- * default; 1 = shared-memory row blocks).  Results agree within the FP64
- * bound of the parity tests; the choice only changes speed. */
+ * default; 1 = shared-memory row blocks.  COO / SCOO: 0 = direct kernels
+ * over a derived row pointer, 1 = merge path.  ELL: 0 = warp tiles of 128
+ * rows, lane l taking rows l, l+32, l+64, l+96, the default; 1 = four
+ * consecutive rows per thread, bit-identical results).  Results agree within
+ * the FP64 bound of the parity tests; the choice only changes speed. */
 tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
 
 /* Tunable knobs of a handle's kernels (what the autotuner sets); results do

@@ -708,6 +708,12 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant) {
     A->csr_variant = variant;
     return TBSLA_OK;
   }
+  if (A->format == TBSLA_FMT_ELL) {
+    TB_CHECK(variant == 0 || variant == 1, "ELL kernel variant %d unknown (0 warp tiles, 1 four rows per thread)",
+             variant);
+    A->csr_variant = variant;
+    return TBSLA_OK;
+  }
   TB_CHECK(variant == 0, "format %d has a single kernel", A->format);
   return TBSLA_OK;
 }

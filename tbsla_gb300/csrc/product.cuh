@@ -188,14 +188,28 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
     break;
   case TBSLA_FMT_ELL:
     if (A->rows > 0 && A->max_col > 0) {
-      const int threads = (A->rows + 3) / 4;
+      const bool cs = A->x_extent * (int64_t)sizeof(XT) <= (64ll << 20);
       KernelTimer kt(A, s);
-      if (A->x_extent * (int64_t)sizeof(XT) <= (64ll << 20))
-        ell_kernel<V, XT, Epi, true><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                           A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
-      else
-        ell_kernel<V, XT, Epi, false><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
-                                                                            A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
+      if (A->csr_variant == 0) {
+        // warp tiles of 128 rows (the default)
+        const int64_t threads = ((int64_t)A->rows + 127) / 128 * 32;
+        const int grid = (int)((threads + 255) / 256);
+        if (cs)
+          ell_warp_kernel<V, XT, Epi, true><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows, A->rows_pad,
+                                                                 A->max_col, xkeep_of<XT>(A), epi);
+        else
+          ell_warp_kernel<V, XT, Epi, false><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows, A->rows_pad,
+                                                                  A->max_col, xkeep_of<XT>(A), epi);
+      } else {
+        // four consecutive rows per thread
+        const int threads = (A->rows + 3) / 4;
+        if (cs)
+          ell_kernel<V, XT, Epi, true><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                             A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
+        else
+          ell_kernel<V, XT, Epi, false><<<(threads + 255) / 256, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                              A->rows_pad, A->max_col, xkeep_of<XT>(A), epi);
+      }
       kt.stop();
     }
     break;

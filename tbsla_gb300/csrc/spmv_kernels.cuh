@@ -335,6 +335,82 @@ __global__ void __launch_bounds__(256) ell_kernel(const int *__restrict__ cols,
   epi.block_done(es, blockIdx.x);
 }
 
+// Warp tiles of 128 rows: lane l of a warp sums rows base + l + 32 q
+// (q = 0..3), slot by slot in stored order (the arithmetic of ell_kernel, so
+// results are bit-identical).  Each load instruction covers 32 consecutive
+// rows: the column and value loads stay coalesced (two 128-byte lines per
+// FP64 instruction) and the gathers of a banded matrix touch the lines of 32
+// neighbouring rows, a quarter of the lines of ell_kernel's four
+// consecutive rows per thread (whose 32 lanes span 128 rows per gather).
+template <bool CS, typename T> __device__ __forceinline__ T ld_ell(const T *p);
+template <> __device__ __forceinline__ int ld_ell<true, int>(const int *p) { return ld_stream(p); }
+template <> __device__ __forceinline__ double ld_ell<true, double>(const double *p) { return ld_stream(p); }
+template <> __device__ __forceinline__ float ld_ell<true, float>(const float *p) { return ld_stream(p); }
+template <> __device__ __forceinline__ __nv_bfloat16 ld_ell<true, __nv_bfloat16>(const __nv_bfloat16 *p) {
+  return ld_stream(p);
+}
+template <> __device__ __forceinline__ int ld_ell<false, int>(const int *p) {
+  int v;
+  asm("ld.global.nc.L2::256B.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+template <> __device__ __forceinline__ double ld_ell<false, double>(const double *p) {
+  double v;
+  asm("ld.global.nc.L2::256B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+template <> __device__ __forceinline__ float ld_ell<false, float>(const float *p) {
+  float v;
+  asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+template <> __device__ __forceinline__ __nv_bfloat16 ld_ell<false, __nv_bfloat16>(const __nv_bfloat16 *p) {
+  unsigned short u;
+  asm("ld.global.nc.L2::256B.u16 %0, [%1];" : "=h"(u) : "l"(p));
+  return __ushort_as_bfloat16(u);
+}
+
+template <typename V, typename XT, typename Epi, bool CS>
+__global__ void __launch_bounds__(256) ell_warp_kernel(const int *__restrict__ cols,
+                                                       const V *__restrict__ vals,
+                                                       const XT *__restrict__ x, int f_col, int rows,
+                                                       int rows_pad, int max_col, XKeep x_keep, Epi epi) {
+  using Acc = typename Epi::Acc;
+  if (!epi.active()) return;
+  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * 128;
+  const int lane = threadIdx.x & 31;
+  typename Epi::State es{};
+  if (base < rows) {
+    const uint64_t keep = policy_keep(x_keep, x);
+    const int r0 = (int)base + lane;
+    bool in[4];
+    #pragma unroll
+    for (int q = 0; q < 4; ++q) in[q] = r0 + 32 * q < rows;
+    Acc a[4] = {0, 0, 0, 0};
+    #pragma unroll 4
+    for (int s = 0; s < max_col; ++s) {
+      const size_t off = (size_t)s * rows_pad + r0;
+      int c[4];
+      V v[4];
+      #pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        c[q] = in[q] ? ld_ell<CS>(cols + off + 32 * q) : 0;
+        v[q] = in[q] ? ld_ell<CS>(vals + off + 32 * q) : V(0);
+      }
+      #pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        int idx = c[q] - f_col;
+        if (idx < 0) idx = 0;
+        if (in[q]) a[q] = fma_acc(to_acc(v[q], Acc()), to_acc(ld_keep(x + idx, keep), Acc()), a[q]);
+      }
+    }
+    #pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (in[q]) epi.emit(r0 + 32 * q, a[q], es);
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
 // --------------------------------------------------------------- DENSE
 // Row-major GEMV: each warp handles four rows at once so that every x chunk
 // loaded serves four rows; lanes stride over the columns, then the warp

@@ -187,6 +187,43 @@ def test_csr_kernel_variants(gpu, orc, variant):
         assert_close(m.spmv_host(x), o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"csr variant {variant} {nr}x{nc}")
 
 
+def test_ell_kernel_variants(gpu, orc):
+    """ELL warp tiles (variant 0: lane l of a warp sums rows l, l+32, l+64,
+    l+96 of a 128-row tile) and four consecutive rows per thread (variant 1)
+    sum each row slot by slot: results are bit-identical and within the FP64
+    bound of the oracle.  Row counts that fill no tile, one row, padding
+    slots, columns below f_col (read as x[0]), reduced-precision stores."""
+    rng = np.random.default_rng(12)
+    for (nr, nc, w, f_col) in [(1, 7, 3, 0), (127, 300, 5, 0), (129, 129, 16, 0), (5000, 4000, 9, 2),
+                               (70001, 70001, 12, 0)]:
+        cols = rng.integers(f_col, nc + f_col, (nr, w)).astype(np.int32)
+        vals = rng.standard_normal((nr, w))
+        cols[::7, -1] = 0  # padding slots (column 0, value 0)
+        vals[::7, -1] = 0.0
+        if f_col:
+            cols[::5, 0] = 0  # below f_col: x[0]
+        x = rng.uniform(-1, 1, nc)
+        stores = gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16
+        m = gpu.DeviceMatrix.ell(nr, nc, w, cols.ravel(), vals.ravel(), f_col=f_col, stores=stores)
+        geom = (nr, nc, nr, nc, 0, f_col, 0, 0, 1, 1, w)
+        o = orc.from_layout("ELL", geom, 0, vals.ravel(), cols.ravel(), np.zeros(0, np.int32))
+        so = orc.from_layout("ELL", geom, 0, np.abs(vals).ravel(), cols.ravel(), np.zeros(0, np.int32))
+        got = {}
+        for variant in (0, 1):
+            m.set_variant(variant)
+            y = m.spmv_host(x)
+            assert_close(y, o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"ell variant {variant} {nr}x{nc}")
+            x32 = Dev.of(gpu, x.astype(np.float32))
+            outs = [y]
+            for store in (gpu.F32, gpu.BF16):
+                y32 = Dev(gpu, nr, np.float32)
+                m.spmv_ex(store, gpu.F32, x32.ptr, gpu.F32, y32.ptr)
+                outs.append(y32.get())
+            got[variant] = outs
+        for a, b in zip(got[0], got[1]):
+            assert np.array_equal(a, b)
+
+
 def test_coo_unsorted_duplicates_and_shift(gpu, orc):
     rng = np.random.default_rng(4)
     for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
