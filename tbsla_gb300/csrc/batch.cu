@@ -28,27 +28,45 @@ struct BatchMember {
 
 constexpr int kBatchRows = 256;
 
+// The block-uniform item loop carries the next item's descriptor and member
+// entry (and its mask flag) one iteration ahead: their dependent loads
+// overlap the current rows' sums instead of preceding them.
 template <typename V, typename T>
 __global__ void __launch_bounds__(256) batch_spmv_kernel(const BatchMember *__restrict__ members,
                                                         const int4 *__restrict__ items, int n_items,
                                                         const int *__restrict__ mask) {
   using Acc = typename AccOf<T>::type;
   const uint64_t keep = policy_keep(0.6f);
-  for (int i = blockIdx.x; i < n_items; i += gridDim.x) {
-    const int4 w = items[i];
-    if (mask && mask[w.x] == 0) continue;  // uniform across the block
-    const BatchMember m = members[w.x];
-    const int r = w.y + (int)threadIdx.x;
-    if (r >= w.z) continue;
-    T *y = static_cast<T *>(m.y);
-    if (r >= m.rows) {
-      y[r] = T(0);
-      continue;
+  int i = blockIdx.x;
+  if (i >= n_items) return;
+  int4 w = items[i];
+  BatchMember m = members[w.x];
+  bool on = !mask || mask[w.x] != 0;
+  for (; i < n_items; i += gridDim.x) {
+    const int in = i + gridDim.x;
+    int4 wn = w;
+    BatchMember mn = m;
+    bool onn = on;
+    if (in < n_items) {
+      wn = items[in];
+      mn = members[wn.x];
+      onn = !mask || mask[wn.x] != 0;
     }
-    const int a = __ldg(m.rowptr + r), b = __ldg(m.rowptr + r + 1);
-    const Acc s = row_sum_thread<V, T, Acc>(m.colidx, static_cast<const V *>(m.values),
-                                            static_cast<const T *>(m.x), m.f_col, a, b, keep);
-    __stcs(y + r, (T)s);
+    const int r = w.y + (int)threadIdx.x;
+    if (on && r < w.z) {  // `on` is uniform across the block
+      T *y = static_cast<T *>(m.y);
+      if (r >= m.rows) {
+        y[r] = T(0);
+      } else {
+        const int a = __ldg(m.rowptr + r), b = __ldg(m.rowptr + r + 1);
+        const Acc s = row_sum_thread<V, T, Acc>(m.colidx, static_cast<const V *>(m.values),
+                                                static_cast<const T *>(m.x), m.f_col, a, b, keep);
+        __stcs(y + r, (T)s);
+      }
+    }
+    w = wn;
+    m = mn;
+    on = onn;
   }
 }
 
