@@ -37,14 +37,16 @@ __global__ void __launch_bounds__(256) grad_short_kernel(const int *__restrict__
 // All rows short and consecutive: a warp takes 32 rows [r0, r0 + 32) and
 // strides its lanes over the segment's entries, so index loads and gradient
 // stores are coalesced; a lane finds the row of its entry by a binary search
-// over the 32 row starts held one per lane (shuffles).  The entry loop runs
-// in whole warps (inactive lanes search too, then store nothing), as the
-// full-mask shuffles require.
+// over the 32 row starts held one per lane (shuffles).  Four strides of the
+// warp go together (128 entries: their index loads, then their gathers, in
+// flight at once).  The entry loop runs in whole warps (inactive lanes
+// search too, then store nothing), as the full-mask shuffles require.
 template <typename T>
 __global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *__restrict__ rowptr,
                                                           const int *__restrict__ colidx, int f_col,
                                                           const T *__restrict__ a, const T *__restrict__ b,
                                                           T scale, T *__restrict__ out) {
+  constexpr int U = 4;
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < rows; w += nwarps) {
@@ -54,17 +56,32 @@ __global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *
     const T ar = r0 + lane < rows ? scale * a[r0 + lane] : T(0);
     const int first = __shfl_sync(0xffffffffu, start, 0);
     const int end = __ldg(rowptr + min(r0 + 32, rows));
-    for (int e0 = first; e0 < end; e0 += 32) {
-      const int e = e0 + lane;
-      int j = 0;  // largest lane index with start <= e
+    for (int e0 = first; e0 < end; e0 += 32 * U) {
+      int col[U];
+      T bv[U];
       #pragma unroll
-      for (int step = 16; step >= 1; step >>= 1) {
-        const int cand = j + step;
-        const int v = __shfl_sync(0xffffffffu, start, cand & 31);
-        if (cand < 32 && v <= e) j = cand;
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + 32 * u + lane;
+        col[u] = e < end ? ld_stream(colidx + e) : f_col;
       }
-      const T arow = __shfl_sync(0xffffffffu, ar, j);
-      if (e < end) out[e] = arow * b[__ldg(colidx + e) - f_col];
+      #pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + 32 * u + lane;
+        bv[u] = e < end ? __ldg(b + (col[u] - f_col)) : T(0);
+      }
+      #pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + 32 * u + lane;
+        int j = 0;  // largest lane index with start <= e
+        #pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int cand = j + step;
+          const int v = __shfl_sync(0xffffffffu, start, cand & 31);
+          if (cand < 32 && v <= e) j = cand;
+        }
+        const T arow = __shfl_sync(0xffffffffu, ar, j);
+        if (e < end) __stcs(out + e, arow * bv[u]);
+      }
     }
   }
 }
