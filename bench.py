@@ -567,10 +567,18 @@ def differentiation_bench(capi, scale=22):
         "fd_edges": 16, "fd_rel_err_max": float(max(errs)), "fd_rel_err_median": float(np.median(errs))}
     G.close()
     torch.cuda.empty_cache()
-    # backward of y = A x, cqmat 2^24, FP32
+    # backward of y = A x, cqmat 2^24, FP32, with the format sweep's L2
+    # settings (64 MiB set-aside holding all of the FP32 vector gathered by
+    # the transposed product; restored after)
     N = N_HEADLINE
+    L = capi.lib()
+    sa0, sa_max = C.c_size_t(), C.c_size_t()
+    capi.check(L.tbsla_get_l2_persisting(C.byref(sa0), C.byref(sa_max)))
+    capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
     A = capi.DeviceMatrix.generate("CSR", "cqmat", N, N, C_HEADLINE, Q_HEADLINE, 0,
                                    stores=capi.STORE_F64 | capi.STORE_F32)
+    A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_FP32)  # before the transposed copy is built: it inherits them
+    A.tune(capi.TUNE_X_L2_RANGE, X_RANGE_HEADLINE)
     st = int(A.info().stored)
     gy = torch.rand(N, dtype=torch.float32, device=dev)
     xv = torch.rand(N, dtype=torch.float32, device=dev)
@@ -603,8 +611,10 @@ def differentiation_bench(capi, scale=22):
     out["spmv_backward_cqmat_2^24_f32"] = {
         "stored": st, "grad_values_ms": round(gv_ms, 4), "grad_values_GB_s": round(gv_bytes / gv_ms / 1e6, 1),
         "transpose_product_ms": round(tr_ms, 4), "transpose_product_GB_s": round(tr_bytes / tr_ms / 1e6, 1),
-        "transpose_build_s": round(build_s, 2)}
+        "transpose_build_s": round(build_s, 2),
+        "l2": "64 MiB persisting set-aside, all of the FP32 vector evict-last"}
     A.close()
+    capi.check(L.tbsla_set_l2_persisting(sa0.value))
     torch.cuda.empty_cache()
     return out
 

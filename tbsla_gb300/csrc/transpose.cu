@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) grad_short_kernel(const int *__restrict__
 // stores are coalesced; a lane finds the row of its entry by a binary search
 // over the 32 row starts held one per lane (shuffles).  Four strides of the
 // warp go together (128 entries: their index loads, then their gathers, in
-// flight at once).  The entry loop runs in whole warps (inactive lanes
+// flight at once; eight measured the same).  The entry loop runs in whole warps (inactive lanes
 // search too, then store nothing), as the full-mask shuffles require.
 template <typename T>
 __global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *__restrict__ rowptr,
