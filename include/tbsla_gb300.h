@@ -157,9 +157,13 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         range policy); 0 (default): a fraction of the
  *                         lines touched.
  *   TBSLA_TUNE_SHORT_ROWS the kernel for rows of at most 32 entries:
- *                         -1 (default) 2 for plain products of FP64 values
- *                         when the short rows average 8 entries or more, 0
- *                         otherwise (PageRank sweeps, FP32 / BF16 stores);
+ *                         -1 (default) for plain products: when every row
+ *                         has at most 4 entries, warp tiles of 64 or 128
+ *                         rows, lane l taking rows l, l+32, ... (one thread
+ *                         per row's arithmetic, bit-identical to 0); else 2
+ *                         for FP64 values when the short rows average 8
+ *                         entries or more; 0 otherwise (and for PageRank
+ *                         sweeps);
  *                         0 one thread per row, summed in stored
  *                         order; 1 (every row short) each 32-row tile's
  *                         entries staged in shared memory with coalesced

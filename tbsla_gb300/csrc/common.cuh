@@ -91,6 +91,7 @@ struct tbsla_matrix {
   int *short_rows = nullptr;
   int n_short = 0;
   int64_t short_nnz = 0;  // entries of the short rows
+  int short_max = 0;      // entries of the longest short row
   // all rows short: shared-memory slots per warp of the staged kernel (the
   // entries of the largest 32-row tile, a multiple of 16); 0 otherwise
   int stage_cap = 0;

@@ -225,6 +225,67 @@ __global__ void __launch_bounds__(256) csr_pair_kernel(const int *__restrict__ r
   epi.block_done(es, blockIdx.x);
 }
 
+// Tiny rows: every row in order and at most T entries (T = 2 or 4).  A warp
+// takes a tile of 32 R rows (R = 8 / T), lane l rows l, l + 32, ..., so
+// each load instruction covers 32 consecutive rows; a lane has the bounds,
+// entries and gathers of its R rows in flight together (one row per thread
+// leaves three dependent loads per row in flight: cdiag rows of two entries
+// stayed latency-bound at two thirds of the HBM rate).  Each row is summed
+// in stored order, one FMA per entry: the one-thread-per-row arithmetic.
+constexpr int kTinyRow = 4;
+
+template <int T, typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_tiny_kernel(int n_rows, const int *__restrict__ rowptr,
+                                                      const int *__restrict__ colidx,
+                                                      const V *__restrict__ values,
+                                                      const XT *__restrict__ x, int f_col, XKeep x_keep,
+                                                      Epi epi) {
+  using Acc = typename Epi::Acc;
+  constexpr int R = 8 / T;
+  if (!epi.active()) return;
+  typename Epi::State es{};
+  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * (32 * R);
+  if (base < n_rows) {
+    const uint64_t keep = policy_keep(x_keep, x);
+    const int r0 = (int)base + (threadIdx.x & 31);
+    int a[R], b[R];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int r = r0 + 32 * q;
+      a[q] = r < n_rows ? __ldg(rowptr + r) : 0;
+      b[q] = r < n_rows ? __ldg(rowptr + r + 1) : 0;
+    }
+    V v[R][T];
+    int c[R][T];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      #pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const int k = a[q] + t;
+        const bool in = k < b[q];
+        c[q][t] = in ? ld_ell<false>(colidx + k) : f_col;  // read-only, 256-byte L2 prefetch
+        v[q][t] = in ? ld_ell<false>(values + k) : V(0);
+      }
+    }
+    Acc xv[R][T];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      #pragma unroll
+      for (int t = 0; t < T; ++t)
+        xv[q][t] = a[q] + t < b[q] ? to_acc(ld_keep(x + (c[q][t] - f_col), keep), Acc()) : Acc(0);
+    }
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      Acc acc = 0;
+      #pragma unroll
+      for (int t = 0; t < T; ++t)
+        if (a[q] + t < b[q]) acc = fma_acc(to_acc(v[q][t], Acc()), xv[q][t], acc);
+      if (r0 + 32 * q < n_rows) epi.emit(r0 + 32 * q, acc, es);
+    }
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
 // sum of entries [a, b) by a group of L lanes of one warp (L a power of two
 // <= 32, groups aligned in the warp): lanes stride the range, fixed shuffle
 // tree within the group.  Valid in the group's first lane.

@@ -424,9 +424,15 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     int slot = 0;
     bool all_short = true;
     int64_t short_nnz = 0;
+    int short_max = 0;
     for (int r = 0; r < rows; ++r) {
       const int len = rp[r + 1] - rp[r];
-      if (len <= kShortRow) { shorts.push_back(r); short_nnz += len; continue; }
+      if (len <= kShortRow) {
+        shorts.push_back(r);
+        short_nnz += len;
+        short_max = std::max(short_max, len);
+        continue;
+      }
       all_short = false;
       if (len <= kChunk) {
         int c = 0;
@@ -446,6 +452,7 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     A->item_class_start[kGroupClasses] = (int)items.size();
     A->n_short = (int)shorts.size();
     A->short_nnz = short_nnz;
+    A->short_max = short_max;
     // staged kernel (all rows short): entries of the largest 32-row tile,
     // rounded up to the 16-entry swizzle group
     A->stage_cap = 0;

@@ -108,6 +108,20 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
     base += short_grid(A->n_short, Epi::kReduces);
     csr_stage_kernel<V, XT, Epi><<<grid, kStageWarps * 32, smem, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
                                                                      xkeep_of<XT>(A), A->stage_cap, epi);
+  } else if (A->n_short > 0 && A->short_rows == nullptr && A->short_mode < 0 && !Epi::kReduces &&
+             A->short_max <= kTinyRow) {
+    // every row in order and tiny: warp tiles of 32 * 8 / T rows
+    const int T = A->short_max <= 2 ? 2 : 4;
+    const int64_t warps = ((int64_t)A->n_short + 32 * (8 / T) - 1) / (32 * (8 / T));
+    const int grid = (int)((warps * 32 + 255) / 256);
+    epi.set_part_base(base);
+    base += short_grid(A->n_short, Epi::kReduces);
+    if (T == 2)
+      csr_tiny_kernel<2, V, XT, Epi><<<grid, 256, 0, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
+                                                          xkeep_of<XT>(A), epi);
+    else
+      csr_tiny_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
+                                                          xkeep_of<XT>(A), epi);
   } else if (A->n_short > 0 && (A->short_mode == 2 || (A->short_mode < 0 && sizeof(V) == 8 && !Epi::kReduces &&
                                                        A->short_nnz >= (int64_t)kPairMinRow * A->n_short))) {
     // two lanes per row: twice the threads of the one-lane grid (reducing

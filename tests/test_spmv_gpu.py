@@ -224,6 +224,36 @@ def test_ell_kernel_variants(gpu, orc):
             assert np.array_equal(a, b)
 
 
+def test_csr_tiny_rows_kernel(gpu, orc):
+    """Rows of at most 4 entries, all in order: warp tiles (lane l taking
+    rows l, l+32, ...) sum each row in stored order, one FMA per entry, so
+    the default product equals one thread per row (TBSLA_TUNE_SHORT_ROWS 0)
+    bit for bit, for every store; ragged rows (0 to 4 entries), row counts
+    that fill no tile, and the FP64 bound against the oracle."""
+    rng = np.random.default_rng(21)
+    for (nr, nc, top) in [(1, 5, 2), (63, 70, 2), (129, 129, 2), (4097, 3000, 4), (200003, 150000, 3),
+                          (70000, 90000, 1)]:
+        lens = rng.integers(0, top + 1, nr)
+        rp, ci, va = random_csr(rng, nr, nc, lens)
+        x = rng.uniform(-1, 1, nc)
+        stores = gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16
+        m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=stores)
+        ref = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=stores)
+        ref.tune(gpu.TUNE_SHORT_ROWS, 0)
+        o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+        so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+        y = m.spmv_host(x)
+        assert_close(y, o.spmv(x), so.spmv(np.abs(x)), RTOL64, f"tiny rows {nr}x{nc}")
+        assert np.array_equal(y, ref.spmv_host(x))
+        assert np.array_equal(m.a_axpx_host(x[:nr]) if nr == nc else y, ref.a_axpx_host(x[:nr]) if nr == nc else y)
+        x32 = Dev.of(gpu, x.astype(np.float32))
+        for store in (gpu.F32, gpu.BF16):
+            ya, yb = Dev(gpu, nr, np.float32), Dev(gpu, nr, np.float32)
+            m.spmv_ex(store, gpu.F32, x32.ptr, gpu.F32, ya.ptr)
+            ref.spmv_ex(store, gpu.F32, x32.ptr, gpu.F32, yb.ptr)
+            assert np.array_equal(ya.get(), yb.get())
+
+
 def test_coo_unsorted_duplicates_and_shift(gpu, orc):
     rng = np.random.default_rng(4)
     for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
