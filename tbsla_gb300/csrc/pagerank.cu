@@ -112,7 +112,6 @@ template <typename YT, typename AccT> struct PrEpi {
   __host__ __device__ void set_part_base(int k) { part_base = k; }
   __device__ __forceinline__ void emit(int row, Acc v, State &st) const {
     if (row < 0 || row >= n) return;
-    double val;
     const double beta = *betap;
     if constexpr (std::is_same<AccT, float>::value) {
       // inner sweep (kSweepInner): e' = beta*G~e + add + r in FP32
@@ -121,19 +120,19 @@ template <typename YT, typename AccT> struct PrEpi {
       if (dmask && dmask[row]) st.b += f;
       st.c += f;
       __stcs(y + row, (YT)f);
-      return;
     } else {
       const double t = mode == kSweepTele ? *add * tvec[row]
                        : (mode == kSweepRef && tmask) ? (tmask[row] ? *add : 0.0) : *add;
-      val = __fma_rn(beta, (double)v, t);
-      if (mode == kSweepRef) st.a = fmax(st.a, val);
-      else st.a += fabs(val - (double)xold[row]);
+      const double val = __fma_rn(beta, (double)v, t);
+      if (mode == kSweepRef) {
+        st.a = fmax(st.a, val);
+      } else {
+        st.a += fabs(val - (double)xold[row]);
+        if (dmask && dmask[row]) st.b += val;
+        st.c += val;
+      }
+      __stcs(y + row, (YT)val);
     }
-    if (mode != kSweepRef) {
-      if (dmask && dmask[row]) st.b += val;
-      st.c += val;
-    }
-    __stcs(y + row, (YT)val);
   }
   __device__ __forceinline__ void block_done(State &st, int blk) const {
     block_reduce3((double)st.a, (double)st.b, (double)st.c, mode == kSweepRef, partials, part_base + blk);
