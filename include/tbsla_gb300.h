@@ -79,12 +79,12 @@ int tbsla_version(void);
 tbsla_status_t tbsla_set_device(int device);
 /* The current device's L2 fetch granularity for this process (the CUDA
  * context limit cudaLimitMaxL2FetchGranularity; 32, 64 or 128 bytes): how
- * much a missing load brings from DRAM.  The short-row CSR kernel asks for
- * 256-byte prefetches on its streamed row data, so at 32 bytes the random
- * gathers of x stop bringing unused sectors while the streams stay wide
- * (cqmat 2^24 FP64: 4396 GB/s at 32 against 4283 at the context's default).
- * Kernels that stream without such hints (the long-row and ELL kernels) lose
- * at 32; the setting is the caller's, process-wide, and ends with it. */
+ * much a missing load brings from DRAM.  The kernels ask for 256-byte
+ * prefetches on their streamed row data, so at 32 bytes the random gathers
+ * of x stop bringing unused sectors while the streams stay wide (cqmat 2^24
+ * FP64, one thread per row: 4396 GB/s at 32 against 4283 at the context's
+ * default; ELL 4741 against 4102).  The setting is the caller's,
+ * process-wide, and ends with it. */
 tbsla_status_t tbsla_set_l2_fetch_granularity(int bytes);
 tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes);
 /* The current device's persisting L2 set-aside for this process (the CUDA
@@ -92,9 +92,10 @@ tbsla_status_t tbsla_get_l2_fetch_granularity(int *bytes);
  * reports its maximum in *max_bytes).  Lines loaded with an evict-last
  * policy -- the gathered x, TBSLA_TUNE_X_L2_KEEP -- stay there ahead of the
  * streamed matrix.  cqmat 2^24 FP64 with all of x evict-last: 5085 GB/s at
- * 64 MiB against 4811 at the context's default (25 MB here); the maximum
- * (84 MB) leaves the streams too little L2 (2920 GB/s), and R-MAT PageRank
- * sweeps lose 2 % at 64 MiB.  Setting it first returns every persisting
+ * 64 MiB against 4811 at the context's default (25 MB here); with the first
+ * 45 % of x's addresses (TBSLA_TUNE_X_L2_RANGE): 5191.  The maximum (84 MB)
+ * leaves the streams too little L2 (2920 GB/s), and R-MAT PageRank sweeps
+ * lose 2 % at 64 MiB.  Setting it first returns every persisting
  * line to normal (cudaCtxResetPersistingL2Cache).  Process-wide, the
  * caller's to set and restore. */
 tbsla_status_t tbsla_set_l2_persisting(size_t bytes);
