@@ -68,21 +68,26 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   const float keeps[] = {0.0f, 0.3f, 0.6f, 1.0f};
   // kernels: 0 direct, 1 row blocks (CSR), 2 direct with the staged
   // short-row kernel (every row at most 32 entries), 3 direct with two lanes
-  // per short row
+  // per short row, 4 direct with warp tiles of tiny rows (every row at most
+  // kTinyRow entries, in order: the default rule, TBSLA_TUNE_SHORT_ROWS -1)
   const bool csr = A->format == TBSLA_FMT_CSR;
+  const bool tiny = A->n_short > 0 && A->short_rows == nullptr && A->short_max <= kTinyRow;
+  auto mode_of = [](int v) { return v == 2 ? 1 : v == 3 ? 2 : v == 4 ? -1 : 0; };
   float best = 1e30f;
-  int best_v = A->csr_variant == 1 ? 1 : A->short_mode == 1 ? 2 : A->short_mode == 2 ? 3 : 0;
+  int best_v = A->csr_variant == 1 ? 1 : A->short_mode == 1 ? 2 : A->short_mode == 2 ? 3
+               : (A->short_mode < 0 && tiny) ? 4 : 0;
   const int mode_in = A->short_mode;
   float best_k = A->x_keep;
   tbsla_status_t st = TBSLA_OK;
   int tried = 0;
-  for (int v = 0; v < 4 && st == TBSLA_OK; ++v) {
+  for (int v = 0; v < 5 && st == TBSLA_OK; ++v) {
     if (v == 1 && !csr) continue;
     if (v == 2 && A->stage_cap == 0) continue;
     if (v == 3 && A->n_short == 0) continue;
+    if (v == 4 && !tiny) continue;
     for (float k : keeps) {
       if (csr) A->csr_variant = v == 1 ? 1 : 0;
-      A->short_mode = v == 2 ? 1 : v == 3 ? 2 : 0;
+      A->short_mode = mode_of(v);
       A->x_keep = k;
       float ms = 0;
       st = time_ms(s, 5, [&] { return tbsla_spmv_ex(A, store, vt, x, vt, y, 0, s); }, &ms);
@@ -97,7 +102,7 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   cudaFree(x);
   cudaFree(y);
   if (csr) A->csr_variant = best_v == 1 ? 1 : 0;
-  A->short_mode = best_v == 2 ? 1 : best_v == 3 ? 2 : 0;
+  A->short_mode = mode_of(best_v);
   if (tried == 0) A->short_mode = mode_in;
   if (A->pr_relabel) A->pr_relabel->short_mode = A->short_mode;
   A->x_keep = best_k;

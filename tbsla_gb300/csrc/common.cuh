@@ -53,6 +53,11 @@ struct DeviceBuffer {
 
 }  // namespace tbsla
 
+namespace tbsla {
+// rows of at most this many entries, all in order: csr_tiny_kernel
+constexpr int kTinyRow = 4;
+}  // namespace tbsla
+
 // The opaque matrix handle of the C ABI.
 struct tbsla_matrix {
   int format = 0;
@@ -91,7 +96,8 @@ struct tbsla_matrix {
   int *short_rows = nullptr;
   int n_short = 0;
   int64_t short_nnz = 0;  // entries of the short rows
-  int short_max = 0;      // entries of the longest short row
+  int short_max = 0;      // entries of the longest short row (<= kTinyRow, all rows
+                          // short and in order: the tiny-row warp tiles)
   // all rows short: shared-memory slots per warp of the staged kernel (the
   // entries of the largest 32-row tile, a multiple of 16); 0 otherwise
   int stage_cap = 0;

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(256) csr_pair_kernel(const int *__restrict__ r
 // leaves three dependent loads per row in flight: cdiag rows of two entries
 // stayed latency-bound at two thirds of the HBM rate).  Each row is summed
 // in stored order, one FMA per entry: the one-thread-per-row arithmetic.
-constexpr int kTinyRow = 4;
+// (kTinyRow, the longest row it takes, is in common.cuh.)
 
 template <int T, typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_tiny_kernel(int n_rows, const int *__restrict__ rowptr,

@@ -254,6 +254,20 @@ def test_csr_tiny_rows_kernel(gpu, orc):
             assert np.array_equal(ya.get(), yb.get())
 
 
+def test_autotune_tries_tiny_rows(gpu):
+    """The SpMV autotuner times the tiny-row warp tiles (choice 4) next to
+    one thread per row, row blocks, staged tiles and two lanes per row, each
+    with four x-keep fractions; integer-valued products stay exact."""
+    n = 1 << 16
+    m = gpu.DeviceMatrix.from_generated(gpu.generate("CSR", "cdiag", n, n, 1, 0.0, 0))
+    x = np.arange(n, dtype=np.float64)
+    before = m.spmv_host(x)
+    r = m.autotune_spmv(gpu.F64)
+    # 4 keeps x (direct, staged, pairs, tiny) + 1 row-block run
+    assert r.candidates == 17 and r.choice in (0, 1, 2, 3, 4)
+    assert np.array_equal(m.spmv_host(x), before)
+
+
 def test_coo_unsorted_duplicates_and_shift(gpu, orc):
     rng = np.random.default_rng(4)
     for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
