@@ -409,7 +409,7 @@ tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pager
  * its own when its L1 change is below p->tol or after p->max_iter sweeps;
  * stopped vectors are frozen while the others continue.  The iterates are
  * multiplied in tiles of `tile` vectors (2, 4, 8, 16 or 32; 0 picks one) as one
- * multi-vector product per tile.  Every p->check_every sweeps (0: 8) the
+ * multi-vector product per tile.  Every p->check_every sweeps (0: 4) the
  * stopped vectors are written out and the running ones repacked into as few
  * tiles as hold them; each result equals the vector solved alone bit for
  * bit.  p->precision: TBSLA_F64, or TBSLA_F32

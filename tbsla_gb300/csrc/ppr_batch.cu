@@ -368,7 +368,7 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   // repacked (compaction), so a tile never keeps sweeping for one slow
   // vector while its other lanes idle.  All tiles of a layout sweep in step:
   // the layout's iterates start in x[base] and sweep j reads x[(base+j)&1].
-  const int K = p->check_every > 0 ? p->check_every : 8;
+  const int K = p->check_every > 0 ? p->check_every : 4;  // 4: R-MAT 2^22, 256 vectors, 3-9 % faster than 8
   int cur_tiles = tiles, base = 0;
   std::vector<int> slot_vec((size_t)tiles * KT, -1);  // vector in each slot, -1 for none
   for (int c = 0; c < k; ++c) slot_vec[(size_t)c] = c;
