@@ -456,12 +456,16 @@ class ReferenceMatrix:
     def nnz(self):
         return self.ref.L.ref_get_nnz(self.p)
 
-    @property
-    def arrays(self) -> Arrays:
+    def serialized(self) -> bytes:
+        """The bytes the reference's Matrix*::write produces."""
         n = self.ref.L.ref_serialize(self.p, None, 0)
         buf = C.create_string_buffer(n)
         self.ref.L.ref_serialize(self.p, buf, n)
-        return parse_binary(self.fmt, buf.raw)
+        return buf.raw
+
+    @property
+    def arrays(self) -> Arrays:
+        return parse_binary(self.fmt, self.serialized())
 
     def update_nnz(self):
         self.ref.L.ref_update_nnz(self.p)

@@ -1,0 +1,59 @@
+// The drop-in classes' host side without a GPU: fill a matrix with the
+// reference generators, write it in the reference's binary layout
+// (Matrix*::write), read the file back into a new object (Matrix*::read) and
+// write that object again.  Nothing here builds a device copy.
+//
+//   dropin_files <FMT> <gen: cqmat|cdiag|stochastic> <n_row> <n_col> <c> <q> <seed> <pr> <pc> <NR> <NC>
+//                <first.bin> <second.bin>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <memory>
+#include <string>
+
+#include <tbsla/cpp/MatrixCOO.hpp>
+#include <tbsla/cpp/MatrixCSR.hpp>
+#include <tbsla/cpp/MatrixDENSE.hpp>
+#include <tbsla/cpp/MatrixELL.hpp>
+#include <tbsla/cpp/MatrixSCOO.hpp>
+
+static std::unique_ptr<tbsla::cpp::Matrix> make(const std::string &fmt) {
+  if (fmt == "COO") return std::make_unique<tbsla::cpp::MatrixCOO>();
+  if (fmt == "SCOO") return std::make_unique<tbsla::cpp::MatrixSCOO>();
+  if (fmt == "CSR") return std::make_unique<tbsla::cpp::MatrixCSR>();
+  if (fmt == "ELL") return std::make_unique<tbsla::cpp::MatrixELL>();
+  if (fmt == "DENSE") return std::make_unique<tbsla::cpp::MatrixDENSE>();
+  return nullptr;
+}
+
+int main(int argc, char **argv) {
+  if (argc != 14) {
+    std::fprintf(stderr, "usage: %s FMT GEN n_row n_col c q seed pr pc NR NC first.bin second.bin\n", argv[0]);
+    return 2;
+  }
+  const std::string fmt = argv[1], gen = argv[2];
+  const int n_row = std::atoi(argv[3]), n_col = std::atoi(argv[4]), c = std::atoi(argv[5]);
+  const double q = std::atof(argv[6]);
+  const unsigned seed = (unsigned)std::strtoul(argv[7], nullptr, 10);
+  const int pr = std::atoi(argv[8]), pc = std::atoi(argv[9]), NR = std::atoi(argv[10]), NC = std::atoi(argv[11]);
+  auto m = make(fmt);
+  auto back = make(fmt);
+  if (!m || !back) return 2;
+  if (gen == "cqmat") m->fill_cqmat(n_row, n_col, c, q, seed, pr, pc, NR, NC);
+  else if (gen == "cdiag") m->fill_cdiag(n_row, n_col, c, pr, pc, NR, NC);
+  else if (gen == "stochastic") m->fill_cqmat_stochastic(n_row, n_col, c, q, seed, pr, pc, NR, NC);
+  else return 2;
+  {
+    std::ofstream os(argv[12], std::ios::binary);
+    m->write(os);
+    if (!os) return 3;
+  }
+  {
+    std::ifstream is(argv[12], std::ios::binary);
+    back->read(is);
+    if (!is) return 4;
+  }
+  std::ofstream os(argv[13], std::ios::binary);
+  back->write(os);
+  return os ? 0 : 5;
+}

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import fnv
+from oracle.oracle import parse_binary, write_binary
 
 FORMATS = ["COO", "SCOO", "CSR", "ELL", "DENSE"]
 SHAPES = [(10, 5, 8), (5, 10, 7), (10, 10, 12), (10, 10, 3), (10, 5, 3), (10, 5, 6), (30, 30, 6), (20, 30, 5),
@@ -163,3 +164,27 @@ def test_rmat_oracle_is_deterministic(orc):
     # quadrant frequencies of the top bit follow (a+b, c+d) = (0.76, 0.24)
     top = (s1 >> 9) & 1
     assert abs(top.mean() - 0.24) < 0.03
+
+
+def _same_bytes(mine, raw, fmt, gen, tag):
+    """Equal bytes; the nnz field (bytes 24-31) only where the reference sets it."""
+    if not nnz_defined(fmt, gen, parse_binary(fmt, raw).values.size):
+        raw, mine = raw[:24] + raw[32:], mine[:24] + mine[32:]
+    assert mine == raw, tag
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_binary_writer_matches_reference_bytes(orc, ref, fmt):
+    """write_binary (the layout the drop-in classes' write and the file
+    loaders follow) reproduces the reference's own Matrix*::write output byte
+    for byte, from the reference's arrays and from the oracle's fill (the nnz
+    field where the reference leaves it unset aside, as everywhere)."""
+    for (nr, nc, c) in SHAPES[:6]:
+        for blk in BLOCKS[:3]:
+            raw = ref.fill_cqmat(fmt, nr, nc, c, 0.1, 1, *blk).serialized()
+            assert write_binary(parse_binary(fmt, raw)) == raw, (fmt, nr, nc, c, blk)
+            _same_bytes(write_binary(orc.fill_cqmat(fmt, nr, nc, c, 0.1, 1, *blk).arrays), raw, fmt, "cqmat",
+                        (fmt, "cqmat", nr, nc, c, blk))
+            raw = ref.fill_cdiag(fmt, nr, nc, 2, *blk).serialized()
+            _same_bytes(write_binary(orc.fill_cdiag(fmt, nr, nc, 2, *blk).arrays), raw, fmt, "cdiag",
+                        (fmt, "cdiag", nr, nc, blk))
