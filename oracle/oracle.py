@@ -387,6 +387,8 @@ class Reference:
         L.ref_serialize.restype = C.c_long
         L.ref_deserialize.argtypes = [C.c_int, C.c_char_p, C.c_long]
         L.ref_deserialize.restype = vp
+        L.ref_read_mm.argtypes = [C.c_char_p]
+        L.ref_read_mm.restype = vp
         L.ref_get_nnz.argtypes = [vp]
         L.ref_get_nnz.restype = C.c_long
         L.ref_get_n_row.argtypes = [vp]
@@ -429,6 +431,11 @@ class Reference:
         b = np.ascontiguousarray(idx1, np.int32)
         return self._wrap(self.L.ref_from_arrays(FORMATS[fmt], n_row, n_col, v, v.size, a, a.size, b, b.size),
                           fmt)
+
+    def read_mm(self, path: str):
+        """MatrixCOO::readMM of the reference, or None where it throws."""
+        p = self.L.ref_read_mm(path.encode())
+        return self._wrap(p, "COO") if p else None
 
     def deserialize(self, fmt, buf: bytes):
         return self._wrap(self.L.ref_deserialize(FORMATS[fmt], buf, len(buf)), fmt)

@@ -121,6 +121,19 @@ void *ref_deserialize(int fmt, const char *buf, long n) {
   return m;
 }
 
+// MatrixCOO::readMM (MatrixCOO.cpp:230-292) into a new COO matrix; NULL when
+// the reader throws (kinds it refuses)
+void *ref_read_mm(const char *path) {
+  auto *m = new tbsla::cpp::MatrixCOO();
+  try {
+    m->readMM(path);
+  } catch (...) {
+    delete m;
+    return nullptr;
+  }
+  return static_cast<Matrix *>(m);
+}
+
 long ref_get_nnz(void *m) { return static_cast<Matrix *>(m)->get_nnz(); }
 int ref_get_n_row(void *m) { return static_cast<Matrix *>(m)->get_n_row(); }
 int ref_get_n_col(void *m) { return static_cast<Matrix *>(m)->get_n_col(); }

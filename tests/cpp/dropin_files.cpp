@@ -5,8 +5,10 @@
 //
 //   dropin_files <FMT> <gen: cqmat|cdiag|stochastic> <n_row> <n_col> <c> <q> <seed> <pr> <pc> <NR> <NC>
 //                <first.bin> <second.bin>
+//   dropin_files MM <file.mtx> <out.bin>   MatrixCOO::readMM, then write (exit 6: the reader refused)
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
 #include <fstream>
 #include <memory>
 #include <string>
@@ -27,6 +29,17 @@ static std::unique_ptr<tbsla::cpp::Matrix> make(const std::string &fmt) {
 }
 
 int main(int argc, char **argv) {
+  if (argc == 4 && std::string(argv[1]) == "MM") {
+    tbsla::cpp::MatrixCOO m;
+    try {
+      m.readMM(argv[2]);
+    } catch (const std::exception &) {
+      return 6;
+    }
+    std::ofstream os(argv[3], std::ios::binary);
+    m.write(os);
+    return os ? 0 : 5;
+  }
   if (argc != 14) {
     std::fprintf(stderr, "usage: %s FMT GEN n_row n_col c q seed pr pc NR NC first.bin second.bin\n", argv[0]);
     return 2;
