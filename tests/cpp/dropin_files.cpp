@@ -6,6 +6,9 @@
 //   dropin_files <FMT> <gen: cqmat|cdiag|stochastic> <n_row> <n_col> <c> <q> <seed> <pr> <pc> <NR> <NC>
 //                <first.bin> <second.bin>
 //   dropin_files MM <file.mtx> <out.bin>   MatrixCOO::readMM, then write (exit 6: the reader refused)
+//   dropin_files CONV <FMT> <n_row> <n_col> <c> <q> <seed> <normalize 0|1> <out.bin>
+//                a COO cqmat fill (normalize_columns first when asked), converted to FMT by the
+//                constructor from MatrixCOO, then written
 #include <cstdio>
 #include <cstdlib>
 #include <exception>
@@ -38,6 +41,22 @@ int main(int argc, char **argv) {
     }
     std::ofstream os(argv[3], std::ios::binary);
     m.write(os);
+    return os ? 0 : 5;
+  }
+  if (argc == 10 && std::string(argv[1]) == "CONV") {
+    const std::string fmt = argv[2];
+    tbsla::cpp::MatrixCOO coo;
+    coo.fill_cqmat(std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]), std::atof(argv[6]),
+                   (unsigned)std::strtoul(argv[7], nullptr, 10));
+    if (std::atoi(argv[8])) coo.normalize_columns();
+    std::unique_ptr<tbsla::cpp::Matrix> m;
+    if (fmt == "CSR") m = std::make_unique<tbsla::cpp::MatrixCSR>(coo);
+    else if (fmt == "ELL") m = std::make_unique<tbsla::cpp::MatrixELL>(coo);
+    else if (fmt == "SCOO") m = std::make_unique<tbsla::cpp::MatrixSCOO>(coo);
+    else if (fmt == "DENSE") m = std::make_unique<tbsla::cpp::MatrixDENSE>(coo);
+    else return 2;
+    std::ofstream os(argv[9], std::ios::binary);
+    m->write(os);
     return os ? 0 : 5;
   }
   if (argc != 14) {
