@@ -97,6 +97,27 @@ std::vector<int64_t> row_col_order(const std::vector<int> &row, const std::vecto
   } while (0)
 // geometry of generated arrays (host_gen.h); nnz only where the reference
 // sets it
+// A stored array takes a fill's result the way the reference refills it
+// (clear, then reserve or resize to the new size): its capacity never
+// shrinks, which print() shows.  The generated array is moved in when the old
+// capacity is smaller and the new array is exactly sized.
+template <typename T> inline void refill(std::vector<T> &dst, std::vector<T> &&src) {
+  if (dst.capacity() < src.size() && src.capacity() == src.size()) {
+    dst = std::move(src);
+    return;
+  }
+  dst.clear();
+  dst.reserve(src.size());
+  dst.insert(dst.end(), src.begin(), src.end());
+}
+
+// The cqmat fills of COO, SCOO and CSR end with shrink_to_fit in the
+// reference: their arrays are exactly sized.
+template <typename T> inline void refill_exact(std::vector<T> &dst, std::vector<T> &&src) {
+  dst = std::move(src);
+  dst.shrink_to_fit();
+}
+
 #define TBSLA_TAKE_GENERATED(o)                                                                 \
   do {                                                                                          \
     n_row = (o).geom[0]; n_col = (o).geom[1]; ln_row = (o).geom[2]; ln_col = (o).geom[3];       \

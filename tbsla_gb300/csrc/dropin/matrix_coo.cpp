@@ -233,7 +233,7 @@ void MatrixCOO::fill_cdiag(int n_row_, int n_col_, int cdiag, int pr_, int pc_, 
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_COO, 1, n_row_, n_col_, cdiag, 0.0, 0, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill(values, std::move(o.values)); refill(row, std::move(o.idx0)); refill(col, std::move(o.idx1));
 }
 
 void MatrixCOO::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_, int pc_,
@@ -241,7 +241,7 @@ void MatrixCOO::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_COO, 0, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(row, std::move(o.idx0)); refill_exact(col, std::move(o.idx1));
 }
 
 void MatrixCOO::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_,
@@ -249,7 +249,7 @@ void MatrixCOO::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, u
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_COO, 2, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(row, std::move(o.idx0)); refill_exact(col, std::move(o.idx1));
 }
 
 // MatrixCOO::normalize_columns (MatrixCOO.cpp:385-393): global columns
@@ -375,7 +375,7 @@ void MatrixSCOO::fill_cdiag(int n_row_, int n_col_, int cdiag, int pr_, int pc_,
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_SCOO, 1, n_row_, n_col_, cdiag, 0.0, 0, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill(values, std::move(o.values)); refill(row, std::move(o.idx0)); refill(col, std::move(o.idx1));
 }
 
 void MatrixSCOO::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_, int pc_,
@@ -383,7 +383,7 @@ void MatrixSCOO::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned in
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_SCOO, 0, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(row, std::move(o.idx0)); refill_exact(col, std::move(o.idx1));
 }
 
 void MatrixSCOO::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_,
@@ -391,7 +391,7 @@ void MatrixSCOO::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, 
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_SCOO, 2, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); row = std::move(o.idx0); col = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(row, std::move(o.idx0)); refill_exact(col, std::move(o.idx1));
 }
 
 // MatrixSCOO::normalize_columns (MatrixSCOO.cpp:401-409): columns relative to

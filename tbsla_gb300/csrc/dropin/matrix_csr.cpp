@@ -167,7 +167,7 @@ void MatrixCSR::fill_cdiag(int n_row_, int n_col_, int cdiag, int pr_, int pc_, 
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_CSR, 1, n_row_, n_col_, cdiag, 0.0, 0, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); rowptr = std::move(o.idx0); colidx = std::move(o.idx1);
+  refill(values, std::move(o.values)); refill(rowptr, std::move(o.idx0)); refill(colidx, std::move(o.idx1));
 }
 
 void MatrixCSR::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_, int pc_,
@@ -175,7 +175,7 @@ void MatrixCSR::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_CSR, 0, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); rowptr = std::move(o.idx0); colidx = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(rowptr, std::move(o.idx0)); refill_exact(colidx, std::move(o.idx1));
 }
 
 void MatrixCSR::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_,
@@ -183,7 +183,7 @@ void MatrixCSR::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, u
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_CSR, 2, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values); rowptr = std::move(o.idx0); colidx = std::move(o.idx1);
+  refill_exact(values, std::move(o.values)); refill_exact(rowptr, std::move(o.idx0)); refill_exact(colidx, std::move(o.idx1));
 }
 
 // MatrixCSR::normalize_columns (MatrixCSR.cpp:423-435): each value divided by

@@ -157,7 +157,7 @@ void MatrixELL::fill_cdiag(int n_row_, int n_col_, int cdiag, int pr_, int pc_, 
   detail::check(generate_arrays(TBSLA_FMT_ELL, 1, n_row_, n_col_, cdiag, 0.0, 0, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
   max_col = o.geom[10];
-  values = std::move(o.values); columns = std::move(o.idx0);
+  refill(values, std::move(o.values)); refill(columns, std::move(o.idx0));
 }
 
 void MatrixELL::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_, int pc_,
@@ -166,7 +166,7 @@ void MatrixELL::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int
   detail::check(generate_arrays(TBSLA_FMT_ELL, 0, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
   max_col = o.geom[10];
-  values = std::move(o.values); columns = std::move(o.idx0);
+  refill(values, std::move(o.values)); refill(columns, std::move(o.idx0));
 }
 
 void MatrixELL::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_,
@@ -175,7 +175,7 @@ void MatrixELL::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, u
   detail::check(generate_arrays(TBSLA_FMT_ELL, 2, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
   max_col = o.geom[10];
-  values = std::move(o.values); columns = std::move(o.idx0);
+  refill(values, std::move(o.values)); refill(columns, std::move(o.idx0));
 }
 
 // MatrixELL::normalize_columns (MatrixELL.cpp:406-423): padding slots count
@@ -292,7 +292,7 @@ void MatrixDENSE::fill_cdiag(int n_row_, int n_col_, int cdiag, int pr_, int pc_
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_DENSE, 1, n_row_, n_col_, cdiag, 0.0, 0, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values);
+  refill(values, std::move(o.values));
 }
 
 void MatrixDENSE::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_, int pc_,
@@ -300,7 +300,7 @@ void MatrixDENSE::fill_cqmat(int n_row_, int n_col_, int c, double q, unsigned i
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_DENSE, 0, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values);
+  refill(values, std::move(o.values));
 }
 
 void MatrixDENSE::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q, unsigned int seed_mult, int pr_,
@@ -308,7 +308,7 @@ void MatrixDENSE::fill_cqmat_stochastic(int n_row_, int n_col_, int c, double q,
   GenArrays o;
   detail::check(generate_arrays(TBSLA_FMT_DENSE, 2, n_row_, n_col_, c, q, seed_mult, pr_, pc_, NR_, NC_, o));
   TBSLA_TAKE_GENERATED(o);
-  values = std::move(o.values);
+  refill(values, std::move(o.values));
 }
 
 // MatrixDENSE::normalize_columns (MatrixDENSE.cpp:288-300)
