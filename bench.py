@@ -55,6 +55,9 @@ L2_PERSIST_BYTES = 64 << 20  # persisting L2 set-aside of the headline (tbsla_se
 X_KEEP_HEADLINE = 0.45
 X_RANGE_HEADLINE = 1
 X_KEEP_FP32 = 1.0
+# the headline's timed products rotate over this many x vectors of different
+# content, so that no evict-last line of one product's x is the next one's
+X_BUFFERS = 4
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
@@ -156,12 +159,11 @@ def max_over_ranks(pg, v: float) -> float:
     return float(t.item())
 
 
-def cpu_spmv_baseline(g, steps: int, threads: int):
+def cpu_spmv_baseline(m, n_row, n_col, nnz, steps: int, threads: int):
     """The reference's CSR product restated in oracle/ (OpenMP over rows) on
-    the full matrix; returns (GB/s, seconds per product)."""
-    from oracle.oracle import Oracle
-    m = Oracle().from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
-    x = np.random.default_rng(1).uniform(-1, 1, g.n_col)
+    the full matrix m (an oracle matrix); returns (GB/s, seconds per
+    product)."""
+    x = np.random.default_rng(1).uniform(-1, 1, n_col)
     m.spmv(x, threads=threads)  # first touch
     ts = []
     for _ in range(steps):
@@ -169,27 +171,42 @@ def cpu_spmv_baseline(g, steps: int, threads: int):
         m.spmv(x, threads=threads)
         ts.append(time.perf_counter() - t0)
     t = float(np.median(ts))
-    return csr_bytes(g.n_row, g.n_col, g.values.size) / t / 1e9, t
+    return csr_bytes(n_row, n_col, nnz) / t / 1e9, t
+
+
+def headline_config(log2n: int, nnz: int, world: int) -> dict:
+    """The headline workload's config, the same for both arms."""
+    n = 1 << log2n
+    return {"workload": WORKLOAD.format(log2n=log2n), "n": n, "nnz": nnz, "format": "CSR",
+            "algorithmic_bytes": csr_bytes(n, n, nnz), "parallelism": f"replicas{world}",
+            "l2": f"inputs larger than L2: {csr_bytes(n, n, nnz) / 1e9:.2f} GB streamed per step, no flush needed",
+            "x_buffers": X_BUFFERS,
+            "l2_fetch_granularity_bytes": L2_FETCH_BYTES, "l2_persisting_bytes_requested": L2_PERSIST_BYTES,
+            "x_evict_last": f"first {X_KEEP_HEADLINE:.0%} of x's addresses (range policy)"}
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU product on the machine's host cores: the cqmat matrix
+    built by the oracle's generators (bit-identical to the reference's
+    fill_cqmat) and multiplied by the oracle's CSR loop; nothing of the
+    product library is loaded."""
     if rank != 0:
         return
-    from tbsla_gb300 import build, capi
+    from oracle.oracle import Oracle
     from oracle.oracle import build as obuild
-    build.build()
     obuild(ref=False)
     threads = os.cpu_count() or 1
     n = 1 << args.log2n
-    g = capi.generate("CSR", "cqmat", n, n, C_HEADLINE, Q_HEADLINE, 0)
-    gbs, t = cpu_spmv_baseline(g, max(args.steps, 1), threads)
+    m = Oracle().fill_cqmat("CSR", n, n, C_HEADLINE, Q_HEADLINE, 0)
+    nnz = int(m.h.s.n_values)
+    gbs, t = cpu_spmv_baseline(m, n, n, nnz, max(args.steps, 1), threads)
     line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.format(log2n=args.log2n), "n": n, "nnz": int(g.values.size),
-                       "format": "CSR"},
+            "config": headline_config(args.log2n, nnz, world),
             "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": f"full matrix, median of {max(args.steps, 1)} products"},
+                             "sample": f"full matrix, median of {max(args.steps, 1)} products (oracle CSR loop, "
+                                       f"OpenMP over rows; matrix from the oracle's fill_cqmat)"},
             "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -290,6 +307,55 @@ def format_sweep(capi, peak, log2n=24):
     return out
 
 
+def cfg1_bench(capi, peak):
+    """The CPU-runnable configuration as stated: cqmat n = 100000, c = 10,
+    q = 0.1, duplicates merged, values U(0,1] (generator cqmat_baseline,
+    seed 0), x U[0,1): each format's product and a_axpx_ on the device (the
+    14 MB matrix stays in L2: a latency case, not a roofline one) beside the
+    oracle's products on the host cores."""
+    import torch
+    from oracle.oracle import Oracle, splitmix64_u01
+    n = 100000
+    threads = os.cpu_count() or 1
+    out = {"workload": "cqmat_baseline n=100000 c=10 q=0.1 seed=0 (duplicates merged, values U(0,1])",
+           "l2": "matrix and vectors L2-resident (14 MB)"}
+    x = splitmix64_u01(0, 2, n)
+    orc = Oracle()
+    for fmt in ("CSR", "ELL", "COO", "SCOO"):
+        A = capi.DeviceMatrix.generate(fmt, "cqmat_baseline", n, n, 10, 0.1, 0)
+        i = A.info()
+        ms = time_product(capi, A, capi.F64, capi.F64, n, n, reps=200)
+        ax_ms = time_axpx(capi, A, n, reps=200)
+        if fmt == "CSR":
+            algo = csr_bytes(n, n, i.stored)
+        elif fmt == "ELL":
+            algo = i.stored * 12 + 2 * n * 8
+        else:
+            algo = i.stored * 16 + 2 * n * 8
+        g = capi.generate(fmt, "cqmat_baseline", n, n, 10, 0.1, 0)
+        om = orc.from_layout(fmt, g.geom, g.nnz, g.values, g.idx0, g.idx1)
+        om.spmv(x, threads=threads)
+        ts = []
+        for _ in range(20):
+            t0 = time.perf_counter()
+            om.spmv(x, threads=threads)
+            ts.append(time.perf_counter() - t0)
+        cpu_ms = float(np.median(ts)) * 1e3
+        # the drop-in's own call: host vectors in, host vector out
+        A.spmv_host(x)
+        t0 = time.perf_counter()
+        for _ in range(50):
+            A.spmv_host(x)
+        host_ms = (time.perf_counter() - t0) / 50 * 1e3
+        out[fmt] = {"stored": int(i.stored), "ms": round(ms, 4), "GB_s": round(algo / ms / 1e6, 1),
+                    "a_axpx_ms": round(ax_ms, 4), "spmv_host_ms": round(host_ms, 4),
+                    "cpu_ms": round(cpu_ms, 3),
+                    "cpu_threads": threads if fmt in ("CSR", "ELL") else 1}
+        A.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def dense_multi(capi, n, k):
     """Y = A X for k vectors (cuBLAS GEMM; tensor cores for the BF16 store)."""
     import torch
@@ -316,9 +382,10 @@ def dense_multi(capi, n, k):
     return res
 
 
-def pagerank_bench(capi, scale=24):
+def pagerank_bench(capi, scale=24, cpu=True):
     """R-MAT 2^scale (16 draws per vertex) PageRank to L1 residual 1e-10:
-    FP64 vs FP32/BF16 + FP64 refinement."""
+    FP64 vs FP32/BF16 + FP64 refinement; the reference mode at 1e-9; with
+    cpu, the oracle's solves on the host cores beside them."""
     import torch
     t0 = time.time()
     A = capi.DeviceMatrix.rmat_pagerank(scale, 16 << scale, 0.57, 0.19, 0.19, seed=1,
@@ -332,7 +399,7 @@ def pagerank_bench(capi, scale=24):
     res = {"graph": f"R-MAT scale {scale}, 2^{scale + 4} draws, (0.57,0.19,0.19,0.05), seed 1", "n": n,
            "edges": int(info.stored), "setup_s": round(setup, 1), "tol": 1e-10,
            "reference_solve": {"tol": 1e-13, "sweeps": r.iterations, "converged": bool(r.converged)}}
-    times = {}
+    times, gpu_vectors = {}, {}
     for name, prec, acc in (("fp64", capi.F64, 0), ("fp32_refined", capi.F32, 0), ("bf16_refined", capi.BF16, 0),
                             ("fp64_anderson", capi.F64, 1)):
         A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec, accel=acc)  # warm: workspace + graphs
@@ -344,15 +411,62 @@ def pagerank_bench(capi, scale=24):
             torch.cuda.synchronize()
             ts.append(time.perf_counter() - t1)
         err = float((out - ref).abs().sum().item())
+        gpu_vectors[name] = out.cpu().numpy()
         times[name] = min(ts)
         res[name] = {"ms": round(min(ts) * 1e3, 2), "sweeps": r.iterations, "fp64_sweeps": r.iterations_f64,
                      "residual": r.residual, "converged": bool(r.converged), "l1_vs_fp64_1e-13": err}
     res["bf16_over_fp64_time"] = round(times["bf16_refined"] / times["fp64"], 3)
     res["anderson_over_fp64_time"] = round(times["fp64_anderson"] / times["fp64"], 3)
     res["fp32_over_fp64_time"] = round(times["fp32_refined"] / times["fp64"], 3)
+    # Matrix::page_rank (reference mode: max-normalised, no dangling term) at
+    # the reference's epsilon 1e-9 on the same graph
+    A.pagerank(out.data_ptr(), beta=0.85, tol=1e-9, max_iter=1000, mode=capi.PR_REFERENCE)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    r = A.pagerank(out.data_ptr(), beta=0.85, tol=1e-9, max_iter=1000, mode=capi.PR_REFERENCE)
+    torch.cuda.synchronize()
+    res["reference_mode_1e-9"] = {"ms": round((time.perf_counter() - t1) * 1e3, 2), "iterations": r.iterations,
+                                  "converged": bool(r.converged)}
+    ref_mode_gpu = out.cpu().numpy()
+    if cpu:
+        res["cpu_baseline"] = pagerank_cpu_baseline(A, gpu_vectors, ref_mode_gpu, res)
     A.close()
     torch.cuda.empty_cache()
     return res
+
+
+def pagerank_cpu_baseline(A, gpu_vectors, ref_mode_gpu, res):
+    """The oracle's PageRank on the host cores, on the graph the GPU solved:
+    the reference's page_rank (Matrix.cpp:13-61, epsilon 1e-9) and the
+    dangling-mode restatement to L1 1e-10, timed; the dangling solve run on
+    to 1e-13 is the anchor each GPU result is compared with (l1_vs_oracle)."""
+    import math
+    from oracle.oracle import Oracle
+    threads = os.cpu_count() or 1
+    orc = Oracle()
+    rp, ci, va = A.csr_download()
+    n = rp.size - 1
+    dang = (np.bincount(ci, minlength=n) == 0).astype(np.uint8)
+    out = {"cores": threads, "kind": "port"}
+    t0 = time.perf_counter()
+    xd, it_d, res_d = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 1e-10, 5000, threads=threads)
+    out["dangling_1e-10"] = {"s": round(time.perf_counter() - t0, 3), "sweeps": it_d, "residual": res_d}
+    xo, it_o, res_o = orc.page_rank_dangling(rp, ci, va, dang, 0.85, 1e-13, 5000, threads=threads)
+    xo = xo / math.fsum(xo)
+    out["anchor"] = {"tol": 1e-13, "sweeps": it_o, "residual": res_o}
+    for name, x in gpu_vectors.items():
+        res[name]["l1_vs_oracle"] = float(np.abs(x - xo).sum())
+    om = orc.from_arrays("CSR", n, n, va, rp, ci)
+    del rp, ci, va
+    t0 = time.perf_counter()
+    b, it = om.page_rank(1e-9, 0.85, 1000, threads=threads)
+    out["reference_mode_1e-9"] = {"s": round(time.perf_counter() - t0, 3), "iterations": it,
+                                  "gpu_iterations_equal": it == res["reference_mode_1e-9"]["iterations"],
+                                  "l1_gpu_vs_oracle": float(np.abs(ref_mode_gpu - b).sum())}
+    out["gpu_speedup_dangling_fp64"] = round(out["dangling_1e-10"]["s"] * 1e3 / res["fp64"]["ms"], 1)
+    out["gpu_speedup_reference_mode"] = round(out["reference_mode_1e-9"]["s"] * 1e3 /
+                                              res["reference_mode_1e-9"]["ms"], 1)
+    return out
 
 
 def _events():
@@ -653,35 +767,40 @@ def run_gb300(args, world, rank, local, pg):
     kernels = A.info().kernels
 
     stream = torch.cuda.Stream()
-    x = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, n)).cuda()
+    # X_BUFFERS vectors of different content, rotated product by product
+    xs_dev = [torch.from_numpy(np.random.default_rng(1 + k).uniform(-1, 1, n)).cuda() for k in range(X_BUFFERS)]
     y = torch.empty(n, dtype=torch.float64, device="cuda")
     sp = stream.cuda_stream
     with torch.cuda.stream(stream):
-        for _ in range(max(args.warmup, 3)):
-            A.spmv(x.data_ptr(), y.data_ptr(), 0, sp)
+        for i in range(max(args.warmup, 3)):
+            A.spmv(xs_dev[i % X_BUFFERS].data_ptr(), y.data_ptr(), 0, sp)
     torch.cuda.synchronize()
-    A.timing(True)
-    A.timing_read()
 
+    def timed(rotate: bool):
+        A.timing(True)
+        A.timing_read()
+        barrier(pg)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for i in range(args.steps):
+                A.spmv(xs_dev[i % X_BUFFERS if rotate else 0].data_ptr(), y.data_ptr(), 0, sp)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(pg)
+        ms = e0.elapsed_time(e1) / args.steps
+        k_ms, k_n = A.timing_read()
+        A.timing(False)
+        return max_over_ranks(pg, ms), k_ms / max(k_n, 1)
+
+    # the same x every product (reported beside the headline)
+    same_step_ms, same_kern_ms = timed(False)
     clk = ClockSampler(local)
     clk.start()
     time.sleep(0.3)
-    barrier(pg)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        for _ in range(args.steps):
-            A.spmv(x.data_ptr(), y.data_ptr(), 0, sp)
-        e1.record(stream)
-    torch.cuda.synchronize()
-    barrier(pg)
-    step_ms = e0.elapsed_time(e1) / args.steps
-    kern_ms, kern_n = A.timing_read()
-    A.timing(False)
+    step_ms, kern_avg_ms = timed(True)
     clocks = clk.stop()
-    step_ms = max_over_ranks(pg, step_ms)
-    kern_avg_ms = kern_ms / max(kern_n, 1)
 
     # end to end through the C ABI with pinned host vectors
     hx, hy = C.c_void_p(), C.c_void_p()
@@ -700,6 +819,7 @@ def run_gb300(args, world, rank, local, pg):
     L.tbsla_host_free(hy)
     capi.check(L.tbsla_set_l2_persisting(sa0.value))
     A.close()
+    del xs_dev
     torch.cuda.empty_cache()
 
     if rank != 0:
@@ -708,23 +828,24 @@ def run_gb300(args, world, rank, local, pg):
     value = world * algo / (step_ms * 1e-3) / 1e9
     achieved = algo / (kern_avg_ms * 1e-3) / 1e9
     threads = os.cpu_count() or 1
-    cpu_gbs, cpu_t = cpu_spmv_baseline(g, 5, threads)
+    from oracle.oracle import Oracle
+    om = Oracle().from_layout("CSR", g.geom, g.nnz, g.values, g.idx0, g.idx1)
     del g
+    cpu_gbs, cpu_t = cpu_spmv_baseline(om, n, n, nnz, 5, threads)
+    del om
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD.format(log2n=args.log2n), "n": n, "nnz": nnz, "format": "CSR",
-                   "algorithmic_bytes": algo,
-                   "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2: 3.56 GB streamed per step, no flush needed",
-                   "l2_fetch_granularity_bytes": L2_FETCH_BYTES,
-                   "l2_persisting_bytes": int(sa_set.value), "x_evict_last": f"first {X_KEEP_HEADLINE:.0%} of x's addresses (range policy)"},
+        "config": headline_config(args.log2n, nnz, world),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": NCU_TRAFFIC_BYTES if args.log2n == 24 else None,
                      "kernel": "csr_pair_kernel", "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel_ms": round(kern_avg_ms, 4)},
+                     "kernel_ms": round(kern_avg_ms, 4), "l2_persisting_bytes_set": int(sa_set.value)},
+        "same_x_every_step": {"value": round(world * algo / (same_step_ms * 1e-3) / 1e9, 2),
+                              "kernel_GB_s": round(algo / (same_kern_ms * 1e-3) / 1e9, 2),
+                              "frac": round(algo / (same_kern_ms * 1e-3) / 1e9 / peak, 4)},
         "cpu_baseline": {"value": round(cpu_gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": "full matrix, median of 5 products (oracle CSR loop, OpenMP over rows)"},
         "e2e": {"value": round(algo / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
@@ -734,6 +855,7 @@ def run_gb300(args, world, rank, local, pg):
         "setup_s": round(setup_s, 2),
     }
     if world == 1 and not args.headline_only:
+        line["cfg1"] = cfg1_bench(capi, peak)
         line["formats"] = format_sweep(capi, peak)
         line["pagerank"] = pagerank_bench(capi)
         line["batching"] = batching_bench(capi)
@@ -751,7 +873,8 @@ def main():
     ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
-    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats"], default=None,
+    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats", "cfg1"],
+                    default=None,
                     help="only one section of the full report (profiling cases)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup()
@@ -764,6 +887,8 @@ def main():
         elif args.section == "batching":
             print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22)}),
                   flush=True)
+        elif args.section == "cfg1":
+            print(json.dumps({"cfg1": cfg1_bench(capi, peaks()[0])}), flush=True)
         elif args.section == "formats":
             print(json.dumps({"formats": format_sweep(capi, peaks()[0], args.log2n)}), flush=True)
         elif args.section == "differentiation":

@@ -178,7 +178,11 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         when the graph is square, has at least 2^20
  *                         vertices, is not banded and its top tenth of
  *                         vertices holds half of the entries.  Results are
- *                         returned in the original labels. */
+ *                         returned in the original labels.  The dangling and
+ *                         mixed-precision modes only: TBSLA_PR_REFERENCE
+ *                         (page_rank, personalized_page_rank) always sweeps
+ *                         the handle itself, so its iteration count follows
+ *                         the reference's summation order at every size. */
 typedef enum {
   TBSLA_TUNE_X_L2_KEEP = 0,
   TBSLA_TUNE_PR_RELABEL = 1,
@@ -480,7 +484,16 @@ tbsla_status_t tbsla_matrix_read_mm(const char *path, int format, tbsla_matrix_t
  *   geom[0..10] = n_row, n_col, ln_row, ln_col, f_row, f_col, pr, pc, NR, NC,
  *   max_col;  *nnz = the reference's nnz field.
  * gen: 0 = cqmat (Matrix*::fill_cqmat), 1 = cdiag (fill_cdiag),
- *      2 = cqmat_stochastic (fill_cqmat_stochastic). */
+ *      2 = cqmat_stochastic (fill_cqmat_stochastic),
+ *      3 = cqmat_baseline: the cqmat pattern of fill_cqmat with duplicates
+ *          merged (each row's columns sorted, repeats kept once) and values
+ *          uniform in (0, 1]: value k in (row, column) order is 1 - u_k with
+ *          u_k = (splitmix64(((uint64_t)1 << 32 | seed_mult) + (k+1) *
+ *          0x9e3779b97f4a7c15) >> 11) * 2^-53 (SplitMix64, Steele, Lea and
+ *          Flood 2014); whole matrix only (pr,pc,NR,NC = 0,0,1,1).  ELL and
+ *          DENSE arrays are those of MatrixELL(COO) / MatrixDENSE(COO).  No
+ *          reference counterpart beyond the pattern: it is the benchmark's
+ *          cqmat with merged duplicates and random values. */
 tbsla_status_t tbsla_generate(int format, int gen, int n_row, int n_col, int c, double q,
                               unsigned int seed_mult, int pr, int pc, int NR, int NC,
                               int64_t sizes[3], int geom[11], int64_t *nnz, double *values,

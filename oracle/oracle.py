@@ -28,6 +28,16 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _up = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
 
+def reference_sources() -> str | None:
+    """The reference's src/cpp directory when it is present on this host:
+    $TBSLA_REF_SRC, else the default of the build recipe (oracle/Makefile)."""
+    path = os.environ.get("TBSLA_REF_SRC")
+    if not path:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref-src"], capture_output=True, text=True)
+        path = r.stdout.strip() if r.returncode == 0 else ""
+    return path if path and os.path.isdir(os.path.join(path, "matrix")) else None
+
+
 def build(ref: bool = True) -> None:
     """Compile liboracle.so (and _ref when the TBSLA sources are present)."""
     targets = ["oracle"] + (["ref"] if ref else [])
@@ -115,6 +125,19 @@ class _Handle:
                       s.nnz, s.pr, s.pc, s.NR, s.NC, s.max_col,
                       _copy(s.values, s.n_values, np.float64), _copy(s.idx0, s.n_idx0, np.int32),
                       _copy(s.idx1, s.n_idx1, np.int32))
+
+
+def splitmix64_u01(seed: int, stream: int, count: int) -> np.ndarray:
+    """u_k in [0, 1), k < count: SplitMix64 (Steele, Lea, Flood, OOPSLA 2014)
+    output k from state (stream << 32) | seed, top 53 bits times 2^-53."""
+    k = np.arange(1, count + 1, dtype=np.uint64)
+    state = np.uint64(((stream & 0xFFFFFFFF) << 32) | (seed & 0xFFFFFFFF))
+    with np.errstate(over="ignore"):
+        z = state + k * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
 
 
 class Oracle:
@@ -244,6 +267,24 @@ class Oracle:
                                          np.ascontiguousarray(x, np.float64), np.ascontiguousarray(w, np.float64),
                                          beta, tol, max_it, gvals.ctypes.data, gv.ctypes.data)
         return gvals, gv, it
+
+    def baseline_cqmat(self, n_row, n_col, c, q, seed=0):
+        """The benchmark's cqmat with merged duplicates and random values
+        (the library's generator 3): the reference's fill_cqmat pattern
+        (MatrixCSR.cpp:299-409, restated here), each (row, column) pair kept
+        once in (row, column) order, value k = 1 - u(seed, stream 1, k).
+        Returns CSR arrays (rowptr, colidx, values)."""
+        a = self.fill_cqmat("CSR", n_row, n_col, c, q, seed).arrays
+        rp, ci = a.rowptr.astype(np.int64), a.colidx.astype(np.int64)
+        rows = np.repeat(np.arange(rp.size - 1, dtype=np.int64), np.diff(rp))
+        key = np.unique(rows * max(n_col, 1) + ci)
+        r = key // max(n_col, 1)
+        col = (key % max(n_col, 1)).astype(np.int32)
+        rowptr = np.zeros(n_row + 1, np.int64)
+        np.add.at(rowptr, r + 1, 1)
+        rowptr = np.cumsum(rowptr).astype(np.int32)
+        values = 1.0 - splitmix64_u01(seed, 1, key.size)
+        return rowptr, col, values
 
     def cqmat_sum_columns(self, nr, nc, c, q, seed_mult):
         s = np.zeros(nc, np.float64)

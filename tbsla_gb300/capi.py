@@ -22,7 +22,7 @@ F64, F32, BF16 = 0, 1, 2
 STORE_F64, STORE_F32, STORE_BF16 = 1, 2, 4
 PR_REFERENCE, PR_DANGLING, PR_TELEPORT = 0, 1, 2
 TUNE_X_L2_KEEP, TUNE_PR_RELABEL, TUNE_X_L2_RANGE, TUNE_SHORT_ROWS = 0, 1, 2, 3
-GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2}
+GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2, "cqmat_baseline": 3}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

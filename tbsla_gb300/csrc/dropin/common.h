@@ -94,6 +94,7 @@ std::vector<int64_t> row_col_order(const std::vector<int> &row, const std::vecto
     n_row = (g).n_row; n_col = (g).n_col; ln_row = (g).ln_row; ln_col = (g).ln_col;             \
     f_row = (g).f_row; f_col = (g).f_col; nnz = (g).nnz; pr = (g).pr; pc = (g).pc;              \
     NR = (g).NR; NC = (g).NC;                                                                   \
+    invalidate_device();                                                                        \
   } while (0)
 // geometry of generated arrays (host_gen.h); nnz only where the reference
 // sets it
@@ -124,4 +125,5 @@ template <typename T> inline void refill_exact(std::vector<T> &dst, std::vector<
     f_row = (o).geom[4]; f_col = (o).geom[5]; pr = (o).geom[6]; pc = (o).geom[7];               \
     NR = (o).geom[8]; NC = (o).geom[9];                                                         \
     if ((o).nnz_set) nnz = (long int)(o).nnz;                                                   \
+    invalidate_device();                                                                        \
   } while (0)

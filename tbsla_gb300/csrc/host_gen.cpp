@@ -395,6 +395,97 @@ tbsla_status_t fill_cdiag(Out &o, int n_row, int n_col, int cd, int pr, int pc, 
   return TBSLA_OK;
 }
 
+// ---------------------------------------------------------- cqmat_baseline
+// The cqmat matrix of the benchmark configuration n = 1e5, c = 10, q = 0.1:
+// the reference's pattern (fill_cqmat, seed_mult as given), duplicates merged
+// (each row's columns sorted, repeats kept once), values drawn uniform in
+// (0, 1].  No reference counterpart beyond the pattern.  Value k (in (row,
+// column) order) is 1 - u(seed_mult, 1, k) with u the SplitMix64 generator
+// (Steele, Lea, Flood, OOPSLA 2014) started at state (stream << 32) | seed:
+// output k = mix(state + (k + 1) * 0x9e3779b97f4a7c15), u = (output >> 11) *
+// 2^-53.  Callers draw x from stream 2 the same way.
+inline u64 splitmix64_at(u64 state, u64 k) {
+  u64 z = state + (k + 1) * 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+tbsla_status_t fill_cqmat_baseline(Out &o, int n_row, int n_col, int c, double q, unsigned s, int pr, int pc,
+                                   int NR, int NC) {
+  if (pr != 0 || pc != 0 || NR != 1 || NC != 1)
+    return tbsla::fail(TBSLA_ERR_INVALID_ARG, "cqmat_baseline is built for the whole matrix (block 0,0 of 1x1)");
+  const int format = o.format;
+  Out csr;
+  csr.format = TBSLA_FMT_CSR;
+  tbsla_status_t st = fill_cqmat(csr, n_row, n_col, c, q, s, 0, 0, 1, 1);
+  if (st != TBSLA_OK) return st;
+  // the fill's rowptr stops after the last row that can hold entries; the
+  // merged matrix has every row (rows past it empty)
+  const i64 filled = csr.idx0.empty() ? 0 : (i64)csr.idx0.size() - 1, rows = n_row;
+  // merge: per row sort the columns, keep each once
+  std::vector<i64> kept((size_t)rows + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (i64 i = 0; i < filled; ++i) {
+    int *b = csr.idx1.data() + csr.idx0[(size_t)i], *e = csr.idx1.data() + csr.idx0[(size_t)i + 1];
+    std::sort(b, e);
+    kept[(size_t)i + 1] = std::unique(b, e) - b;
+  }
+  for (i64 i = 0; i < rows; ++i) kept[(size_t)i + 1] += kept[(size_t)i];
+  const i64 nnz = kept[(size_t)rows];
+  std::vector<int> rowptr((size_t)rows + 1), colidx((size_t)nnz), rowof((size_t)nnz);
+  std::vector<double> values((size_t)nnz);
+  const u64 state = ((u64)1 << 32) | (u64)s;
+  int longest = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(max : longest)
+  for (i64 i = 0; i < rows; ++i) {
+    const i64 b = kept[(size_t)i], len = kept[(size_t)i + 1] - b;
+    rowptr[(size_t)i] = (int)b;
+    if (len == 0) continue;
+    for (i64 j = 0; j < len; ++j) {
+      colidx[(size_t)(b + j)] = csr.idx1[(size_t)(csr.idx0[(size_t)i] + j)];
+      rowof[(size_t)(b + j)] = (int)i;
+      values[(size_t)(b + j)] = 1.0 - (double)(splitmix64_at(state, (u64)(b + j)) >> 11) * 0x1.0p-53;
+    }
+    longest = std::max(longest, (int)len);
+  }
+  rowptr[(size_t)rows] = (int)nnz;
+  o = Out();
+  o.format = format;
+  Block b;
+  set_block(o, b, n_row, n_col, 0, 0, 1, 1);
+  o.nnz = nnz;
+  o.nnz_set = true;
+  switch (format) {
+  case TBSLA_FMT_CSR:
+    o.values = std::move(values); o.idx0 = std::move(rowptr); o.idx1 = std::move(colidx);
+    break;
+  case TBSLA_FMT_COO:
+  case TBSLA_FMT_SCOO:
+    o.values = std::move(values); o.idx0 = std::move(rowof); o.idx1 = std::move(colidx);
+    break;
+  case TBSLA_FMT_ELL: {  // as MatrixELL(const MatrixCOO&): padding (column 0, value 0)
+    o.geom[10] = longest;
+    o.values.assign((size_t)(b.lr * longest), 0.0);
+    o.idx0.assign((size_t)(b.lr * longest), 0);
+    for (i64 i = 0; i < rows; ++i)
+      for (i64 k = rowptr[(size_t)i]; k < rowptr[(size_t)i + 1]; ++k) {
+        const size_t slot = (size_t)(i * longest + (k - rowptr[(size_t)i]));
+        o.values[slot] = values[(size_t)k];
+        o.idx0[slot] = colidx[(size_t)k];
+      }
+    break;
+  }
+  default:  // DENSE, as MatrixDENSE(const MatrixCOO&)
+    o.values.assign((size_t)(b.lr * b.lc), 0.0);
+    for (i64 i = 0; i < rows; ++i)
+      for (i64 k = rowptr[(size_t)i]; k < rowptr[(size_t)i + 1]; ++k)
+        o.values[(size_t)(i * b.lc + colidx[(size_t)k])] += values[(size_t)k];
+    break;
+  }
+  return TBSLA_OK;
+}
+
 }  // namespace
 
 namespace tbsla {
@@ -412,6 +503,7 @@ tbsla_status_t generate_arrays(int format, int gen, int n_row, int n_col, int c,
   if (gen == 0) return fill_cqmat(o, n_row, n_col, c, q, seed_mult, pr, pc, NR, NC);
   if (gen == 1) return fill_cdiag(o, n_row, n_col, c, pr, pc, NR, NC);
   if (gen == 2) return fill_cqmat_stochastic(o, n_row, n_col, c, q, seed_mult, pr, pc, NR, NC);
+  if (gen == 3) return fill_cqmat_baseline(o, n_row, n_col, c, q, seed_mult, pr, pc, NR, NC);
   return fail(TBSLA_ERR_INVALID_ARG, "unknown generator %d", gen);
 }
 

@@ -20,7 +20,8 @@ struct GenArrays {
   std::vector<int> idx0, idx1;
 };
 
-// gen: 0 = cqmat, 1 = cdiag (c is the diagonal offset), 2 = cqmat_stochastic
+// gen: 0 = cqmat, 1 = cdiag (c is the diagonal offset), 2 = cqmat_stochastic,
+// 3 = cqmat_baseline (whole matrix only; see tbsla_generate)
 tbsla_status_t generate_arrays(int format, int gen, int n_row, int n_col, int c, double q,
                                unsigned int seed_mult, int pr, int pc, int NR, int NC,
                                GenArrays &out);

@@ -14,6 +14,8 @@
 // array's device address up with cudaGetSymbolAddress (in host code the
 // array's name is only a host-side stand-in, not a device address).  That
 // first call should therefore come before any stream capture on the device.
+// The address is kept per device with the id of the context it belongs to;
+// a call in another context (after cudaDeviceReset, say) looks it up again.
 //
 // Sharing: every call uses the same array.  Each call overwrites every carry
 // it reads before reading it (nothing has to start at zero; y is cleared by
@@ -22,6 +24,7 @@
 // the caller.
 #include <mutex>
 
+#include "driver.cuh"
 #include "product.cuh"
 
 namespace tbsla {
@@ -41,18 +44,27 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
+// per device: the context the address was looked up in, and the address
+static unsigned long long g_noalloc_ctx[kMaxDevices] = {0};
 static unsigned char *g_noalloc_addr[kMaxDevices] = {nullptr};
 
-// device address of the scratch array on the current device (looked up once)
+// Device address of the scratch array in the current device's current
+// context.  Looked up once per context: after cudaDeviceReset the runtime
+// makes a new context, whose id differs, and the array is looked up again.
 static tbsla_status_t noalloc_scratch(unsigned char **out) {
   int dev = 0;
   TB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(TBSLA_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  unsigned long long ctx = 0;
+  TB_TRY(current_context_id(&ctx));
+  if (!g_noalloc_addr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+    // the lookup made the device's context current if none was
+    TB_TRY(current_context_id(&ctx));
+    g_noalloc_ctx[dev] = ctx;
     g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
   }
   *out = g_noalloc_addr[dev];

@@ -1027,14 +1027,17 @@ static tbsla_status_t adjoint_impl(tbsla_matrix *A, const tbsla_pagerank_params_
 }
 
 // PageRank of A, on its relabelled copy when there is one (pr_relabel.cu);
-// *result points to the vector in A's labels (d_out, or a buffer of A's)
+// *result points to the vector in A's labels (d_out, or a buffer of A's).
+// The reference mode never takes the copy: relabelling reorders every row's
+// sum and the block sums of the max-normalised residual, and the reference's
+// iteration count (Matrix.cpp:13-114) moves with that order near epsilon.
 static tbsla_status_t pagerank_entry(tbsla_matrix *A, const tbsla_pagerank_params_t *p, const int *nodes,
                                      int n_nodes, double *d_out, tbsla_pagerank_result_t *res, cudaStream_t user,
                                      const double **result, const double *d_teleport = nullptr) {
   TB_CHECK(A && p, "NULL argument");
   TB_CUDA(cudaSetDevice(A->device));
   tbsla_matrix *B = nullptr;
-  if (!d_teleport) TB_TRY(pr_relabelled(A, &B));
+  if (!d_teleport && p->mode != TBSLA_PR_REFERENCE) TB_TRY(pr_relabelled(A, &B));
   if (!B) {
     TB_TRY(pagerank_impl(A, p, nodes, n_nodes, d_out, res, user, d_teleport));
     if (result) *result = d_out ? d_out : pr_result(static_cast<PrWork *>(A->pr_work));

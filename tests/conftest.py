@@ -64,8 +64,8 @@ def orc():
 
 @pytest.fixture(scope="session")
 def ref():
-    from oracle.oracle import Reference, build, reference_available
-    if os.path.isdir("/root/reference/src/cpp"):
+    from oracle.oracle import Reference, build, reference_available, reference_sources
+    if reference_sources():
         build(ref=True)
     if not reference_available():
         pytest.skip("reference build oracle/_ref not present on this host")

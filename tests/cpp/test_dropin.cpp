@@ -278,6 +278,63 @@ static void mutation_rebuilds_device_copy() {
   expect(m.spmv(iota_vec(300)).size() == 300, "refill rebuilds the device copy");
 }
 
+// A second fill or read of the same shape reuses the arrays' buffers (same
+// data pointers and sizes); the product after it must be the new matrix's,
+// equal to a fresh object's holding the same fill.
+static std::unique_ptr<Matrix> make_format(const std::string &f) {
+  if (f == "COO") return std::make_unique<MatrixCOO>();
+  if (f == "SCOO") return std::make_unique<MatrixSCOO>();
+  if (f == "CSR") return std::make_unique<MatrixCSR>();
+  if (f == "ELL") return std::make_unique<MatrixELL>();
+  return std::make_unique<MatrixDENSE>();
+}
+
+static void refill_same_shape(const std::string &dir) {
+  const std::vector<double> v = iota_vec(400);
+  using Fill = std::function<void(Matrix &)>;
+  const std::pair<const char *, Fill> fills[] = {
+      {"cqmat seed 1", [](Matrix &m) { m.fill_cqmat(400, 400, 8, 0.1, 1); }},
+      {"cqmat seed 2", [](Matrix &m) { m.fill_cqmat(400, 400, 8, 0.1, 2); }},
+      {"cqmat_stochastic seed 2", [](Matrix &m) { m.fill_cqmat_stochastic(400, 400, 8, 0.1, 2); }},
+      {"cdiag 3", [](Matrix &m) { m.fill_cdiag(400, 400, 3); }},
+      {"cdiag 5", [](Matrix &m) { m.fill_cdiag(400, 400, 5); }},
+      {"cqmat seed 3", [](Matrix &m) { m.fill_cqmat(400, 400, 8, 0.1, 3); }}};
+  for (const char *f : {"COO", "SCOO", "CSR", "ELL", "DENSE"}) {
+    auto m = make_format(f);
+    std::vector<double> prev;
+    for (const auto &fl : fills) {
+      fl.second(*m);
+      const std::vector<double> got = m->spmv(v);
+      auto fresh = make_format(f);
+      fl.second(*fresh);
+      expect(got == fresh->spmv(v), std::string("refill ") + f + " " + fl.first);
+      expect(got != prev, std::string("refill changes the product ") + f + " " + fl.first);
+      prev = got;
+    }
+    // read() of two files of the same shape into one object
+    const std::string p1 = dir + "/refill_a_" + f + ".bin", p2 = dir + "/refill_b_" + f + ".bin";
+    auto a = make_format(f), b = make_format(f);
+    a->fill_cqmat(400, 400, 8, 0.1, 4);
+    b->fill_cqmat(400, 400, 8, 0.1, 5);
+    for (auto &pm : {std::make_pair(&p1, a.get()), std::make_pair(&p2, b.get())}) {
+      std::remove(pm.first->c_str());
+      std::ofstream os(*pm.first, std::ofstream::binary);
+      pm.second->write(os);
+    }
+    auto r = make_format(f);
+    {
+      std::ifstream is(p1, std::ifstream::binary);
+      r->read(is);
+    }
+    expect(r->spmv(v) == a->spmv(v), std::string("read first file ") + f);
+    {
+      std::ifstream is(p2, std::ifstream::binary);
+      r->read(is);
+    }
+    expect(r->spmv(v) == b->spmv(v), std::string("read second file of the same shape ") + f);
+  }
+}
+
 int main(int argc, char **argv) {
   const std::string dir = argc > 1 ? argv[1] : ".";
   const std::pair<const char *, std::function<void()>> sections[] = {
@@ -288,7 +345,8 @@ int main(int argc, char **argv) {
       {"binary_round_trip", [&] { binary_round_trip(dir); }},
       {"matrix_market", [&] { matrix_market(dir); }},
       {"c_abi", [&] { c_abi(dir); }},
-      {"mutation_rebuilds_device_copy", mutation_rebuilds_device_copy}};
+      {"mutation_rebuilds_device_copy", mutation_rebuilds_device_copy},
+      {"refill_same_shape", [&] { refill_same_shape(dir); }}};
   for (const auto &sec : sections) {
     try {
       sec.second();

@@ -28,3 +28,15 @@ def test_reference_arm_prints_the_contract_line():
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm generates and multiplies with the oracle alone: the
+    product library is never loaded into its process."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--log2n', '14', '--steps', '1', "
+            "'--warmup', '1']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('PRODUCT_LOADED', 'libtbsla_gb300' in maps, 'ORACLE_LOADED', 'liboracle' in maps)")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "PRODUCT_LOADED False ORACLE_LOADED True" in r.stdout, r.stdout[-1000:]

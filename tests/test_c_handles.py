@@ -10,8 +10,11 @@ import subprocess
 
 import pytest
 
+from oracle.oracle import reference_sources
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_C_INCLUDE = "/root/reference/src/cpp/interface/c/include"
+_REF_SRC = reference_sources()
+REF_C_INCLUDE = os.path.join(_REF_SRC, "interface", "c", "include") if _REF_SRC else ""
 REF_LIB_DIR = os.path.join(ROOT, "oracle", "_ref")
 
 

@@ -22,9 +22,12 @@ import subprocess
 
 import pytest
 
+from oracle.oracle import reference_sources
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REFERENCE_TESTS = "/root/reference/src/cpp/tests"
+_REF_SRC = reference_sources()
+REFERENCE_TESTS = os.path.join(_REF_SRC, "tests") if _REF_SRC else ""
 
 C_HEADERS = [os.path.join(INCLUDE, "tbsla_gb300.h")] + sorted(glob.glob(os.path.join(INCLUDE, "tbsla", "cpp", "*.h")))
 

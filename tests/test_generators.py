@@ -68,3 +68,43 @@ def test_generate_rejects_bad_arguments(capi):
         capi.generate("CSR", "cqmat", 10, 10, -1, 0.1, 0)
     with pytest.raises(capi.TbslaError):
         capi.generate("CSR", "cqmat", 10, 10, 3, 0.1, 0, pr=2, NR=2)
+
+
+def test_splitmix64_known_answers():
+    """The value stream of cqmat_baseline: SplitMix64 from state 0 gives the
+    generator's published first outputs (Steele, Lea, Flood 2014)."""
+    from oracle.oracle import splitmix64_u01
+    first = [0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4, 0x06C45D188009454F]
+    assert list(splitmix64_u01(0, 0, 3)) == [(v >> 11) * 2.0 ** -53 for v in first]
+
+
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_cqmat_baseline_matches_oracle(capi, orc, fmt):
+    """Generator 3 (the benchmark's cqmat n = 1e5, c = 10, q = 0.1 with merged
+    duplicates and U(0,1] values) against the oracle's restatement: the
+    reference's pattern, unique (row, column) pairs, SplitMix64 values."""
+    shapes = [(100000, 100000, 10, 0.1, 0), (300, 200, 12, 0.5, 3), (200, 300, 7, 1.0, 1)]
+    if fmt == "DENSE":
+        shapes = shapes[1:]
+    for (nr, nc, c, q, s) in shapes:
+        rp, ci, va = orc.baseline_cqmat(nr, nc, c, q, s)
+        assert np.all(va > 0) and np.all(va <= 1)
+        g = capi.generate(fmt, "cqmat_baseline", nr, nc, c, q, s)
+        assert g.nnz == va.size
+        rows = np.repeat(np.arange(nr, dtype=np.int32), np.diff(rp))
+        if fmt == "CSR":
+            assert np.array_equal(g.idx0, rp) and np.array_equal(g.idx1, ci) and np.array_equal(g.values, va)
+        elif fmt in ("COO", "SCOO"):
+            assert np.array_equal(g.idx0, rows) and np.array_equal(g.idx1, ci) and np.array_equal(g.values, va)
+        elif fmt == "ELL":
+            # MatrixELL(const MatrixCOO&) of the merged triplets (the oracle's conversion)
+            e = orc.from_arrays("COO", nr, nc, va, rows, ci).convert("ELL").arrays
+            assert g.max_col == e.max_col and np.array_equal(g.idx0, e.idx0) and np.array_equal(g.values, e.values)
+        else:
+            e = orc.from_arrays("COO", nr, nc, va, rows, ci).convert("DENSE").arrays
+            assert np.array_equal(g.values, e.values)
+    # the raw pattern of the benchmark matrix repeats 11 pairs
+    raw = capi.generate("CSR", "cqmat", 100000, 100000, 10, 0.1, 0)
+    assert raw.values.size - capi.generate("CSR", "cqmat_baseline", 100000, 100000, 10, 0.1, 0).values.size == 11
+    with pytest.raises(capi.TbslaError):
+        capi.generate("CSR", "cqmat_baseline", 10, 10, 3, 0.1, 0, pr=1, NR=2)

@@ -131,14 +131,32 @@ def test_relabelled_pagerank(gpu, orc, scale, mode):
         assert r.converged and rp_.converged
         assert np.abs(x - xo).sum() < 1e-10, (prec, acc)
         assert np.abs(x - xp).sum() < 1e-10, (prec, acc)
-    # reference mode and a personalised node list (labels mapped inside)
-    x, r = A.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
-    xp, rp_ = P.pagerank_host(tol=1e-9, max_iter=500, mode=gpu.PR_REFERENCE)
-    assert abs(r.iterations - rp_.iterations) <= 1 and np.abs(x - xp).sum() < 1e-8
-    nodes = [0, 7, 7, (1 << scale) - 1, 12345 % (1 << scale)]
-    y, r = A.personalized_pagerank_host(nodes, tol=1e-9, max_iter=500)
-    yp, rp_ = P.personalized_pagerank_host(nodes, tol=1e-9, max_iter=500)
-    assert abs(r.iterations - rp_.iterations) <= 1 and np.abs(y - yp).sum() < 1e-8
+
+
+@pytest.mark.parametrize("relabel", [-1, 1])
+def test_reference_mode_large_skewed_against_oracle(gpu, orc, relabel):
+    """Matrix::page_rank / personalized_page_rank (Matrix.cpp:13-114) on a
+    non-banded R-MAT graph of 2^20 vertices, where the dangling mode takes the
+    degree-relabelled copy: the reference mode sweeps the handle itself (with
+    the automatic rule and with relabelling forced), so it stops after the
+    oracle's iteration count with the oracle's vector to 1e-12."""
+    scale = 20
+    m = 16 << scale
+    A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=3)
+    A.tune(gpu.TUNE_PR_RELABEL, relabel)
+    rp, ci, va, _ = rmat_csr_oracle(orc, scale, m, 3)
+    n = 1 << scale
+    o = orc.from_arrays("CSR", n, n, va, rp, ci)
+    for eps in (1e-9, 1e-6):
+        b, r = A.pagerank_host(beta=0.85, tol=eps, max_iter=500, mode=gpu.PR_REFERENCE)
+        bo, it = o.page_rank(eps, 0.85, 500, threads=1)
+        assert r.iterations == it, (eps, r.iterations, it)
+        assert np.abs(b - bo).sum() <= 1e-12, (eps, np.abs(b - bo).sum())
+    nodes = [0, 7, 7, n - 1, 12345]
+    p, r = A.personalized_pagerank_host(nodes, beta=0.85, tol=1e-9, max_iter=500)
+    po, it = o.personalized_page_rank(1e-9, 0.85, 500, nodes, threads=1)
+    assert r.iterations == it, (r.iterations, it)
+    assert np.abs(p - po).sum() <= 1e-12, np.abs(p - po).sum()
 
 
 def test_pagerank_argument_checks(gpu):

@@ -132,6 +132,26 @@ def test_cfg1_all_formats(gpu, orc, fmt):
         assert_close(m.a_axpx_host(x), o.a_axpx(x), scale, 1e-12, f"{fmt} a_axpx")
 
 
+@pytest.mark.parametrize("fmt", FORMATS)
+def test_cfg1_baseline_cqmat_all_formats(gpu, orc, fmt):
+    """The benchmark's cqmat as configured (n = 100000, c = 10, q = 0.1,
+    duplicates merged, values U(0,1], x U[0,1), seed 0; DENSE at n = 3000):
+    every format's product and a_axpx_ against the oracle of the reference's
+    array constructor MatrixCSR(n, n, values, rowptr, colidx)
+    (MatrixCSR.cpp:13-27) and its spmv / a_axpx_."""
+    from oracle.oracle import splitmix64_u01
+    n = 100000 if fmt != "DENSE" else 3000
+    rp, ci, va = orc.baseline_cqmat(n, n, 10, 0.1, 0)
+    o = orc.from_arrays("CSR", n, n, va, rp, ci)
+    oa = orc.from_arrays("CSR", n, n, np.abs(va), rp, ci)
+    x = splitmix64_u01(0, 2, n)
+    A = gpu.DeviceMatrix.generate(fmt, "cqmat_baseline", n, n, 10, 0.1, 0)
+    if fmt in ("COO", "SCOO", "CSR"):
+        assert A.info().stored == va.size
+    assert_close(A.spmv_host(x), o.spmv(x), oa.spmv(x), RTOL64, f"{fmt} baseline-cqmat spmv")
+    assert_close(A.a_axpx_host(x), o.a_axpx(x), oa.spmv(oa.spmv(x) + x), RTOL64, f"{fmt} baseline-cqmat a_axpx_")
+
+
 def random_csr(rng, n_row, n_col, lengths):
     rowptr = np.zeros(n_row + 1, np.int64)
     rowptr[1:] = np.cumsum(lengths)

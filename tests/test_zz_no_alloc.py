@@ -3,10 +3,13 @@
 Callers whose device memory belongs to another allocator, or who cannot
 afford the synchronisation of cudaMalloc/cudaFree, use this entry point: it
 takes the caller's device buffers and keeps its scratch in a fixed array
-inside the library.  The test calls it through the C ABI, twice in a row (the
-array keeps the first call's contents), and compares with the allocating
-path (tbsla_coo_create + tbsla_spmv_host) within the FP64 bound of the other
-parity tests.  It lives in its own file, collected last.
+inside the library.  The tests call it through the C ABI, twice in a row (the
+array keeps the first call's contents), and compare with the allocating
+path (tbsla_coo_create + tbsla_spmv_host) and with the oracle's COO product
+within the FP64 bound of the other parity tests; then at exactly the array's
+capacity followed by a smaller call (stale carries of the larger call must
+not leak into it), with the device's free memory unchanged across warmed-up
+calls.  They live in their own file, collected last.
 """
 import ctypes as C
 
@@ -62,12 +65,62 @@ def test_no_alloc_coo_product_matches_allocating_path(gpu, orc):
     rows, cols, vals = _Dev(gpu, g.idx0), _Dev(gpu, g.idx1), _Dev(gpu, g.values)
     m = gpu.DeviceMatrix.coo(n, n, g.idx0, g.idx1, g.values)
     scale_m = orc.from_arrays("COO", n, n, np.abs(g.values), g.idx0, g.idx1)
+    o = orc.from_arrays("COO", n, n, g.values, g.idx0, g.idx1)
     for call in range(2):
         x = rng.uniform(-1, 1, n)
         dx, dy = _Dev(gpu, x), _Dev(gpu, np.full(n, np.nan))
         gpu.check(f(n, n, g.values.size, rows.p, cols.p, vals.p, dx.p, dy.p, None))
         y = dy.get()
-        assert_close(y, m.spmv_host(x), scale_m.spmv(np.abs(x)), 1e-12, f"no-alloc call {call}")
+        scale = scale_m.spmv(np.abs(x))
+        assert_close(y, m.spmv_host(x), scale, 1e-12, f"no-alloc call {call} vs allocating path")
+        assert_close(y, o.spmv(x), scale, 1e-12, f"no-alloc call {call} vs oracle")
+
+
+# the array's capacity: 16384 tiles of 2304 stored entries
+CAP = 16384 * 2304
+
+
+def _device_free_bytes():
+    """Free device memory seen by the driver in the current context."""
+    L = C.CDLL("libcuda.so.1")
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert L.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+def _banded_coo(n_row, n_col, per_row, seed):
+    """Row-sorted triplets: per_row entries in each row, scattered columns."""
+    rng = np.random.default_rng(seed)
+    row = np.repeat(np.arange(n_row, dtype=np.int32), per_row)
+    col = ((row.astype(np.int64) * 7 + rng.integers(0, n_col, row.size)) % n_col).astype(np.int32)
+    val = rng.uniform(-1, 1, row.size)
+    return row, col, val
+
+
+def test_no_alloc_at_capacity_then_smaller(gpu, orc):
+    f = _noalloc(gpu)
+    rng = np.random.default_rng(5)
+    big_rows = CAP // 16
+    cases = [(big_rows, 1 << 20, 16, 1), (3001, 2000, 7, 2)]
+    runs = []
+    for (nr, nc, per_row, seed) in cases:
+        row, col, val = _banded_coo(nr, nc, per_row, seed)
+        runs.append((nr, nc, row, col, val, _Dev(gpu, row), _Dev(gpu, col), _Dev(gpu, val)))
+    assert runs[0][2].size == CAP  # the last slot of every carry array is used
+    # capacity, smaller, capacity again, smaller again
+    for k, (nr, nc, row, col, val, drow, dcol, dval) in enumerate(runs + runs):
+        x = rng.uniform(-1, 1, nc)
+        dx, dy = _Dev(gpu, x), _Dev(gpu, np.full(nr, np.nan))
+        free_before = _device_free_bytes()
+        gpu.check(f(nr, nc, row.size, drow.p, dcol.p, dval.p, dx.p, dy.p, None))
+        gpu.check(gpu.lib().tbsla_stream_sync(None))
+        free_after = _device_free_bytes()
+        if k >= 2:  # warmed up: the kernels are loaded, nothing else may take memory
+            assert free_after == free_before, (k, free_before - free_after)
+        y = dy.get()
+        o = orc.from_arrays("COO", nr, nc, val, row, col)
+        scale = orc.from_arrays("COO", nr, nc, np.abs(val), row, col).spmv(np.abs(x), threads=8)
+        assert_close(y, o.spmv(x, threads=8), scale, 1e-12, f"no-alloc call {k} ({nr} rows) vs oracle")
 
 
 def test_no_alloc_rejects_oversized_input(gpu):
