@@ -357,27 +357,53 @@ def cfg1_bench(capi, peak):
 
 
 def dense_multi(capi, n, k):
-    """Y = A X for k vectors (cuBLAS GEMM; tensor cores for the BF16 store)."""
+    """Y = A X for k vectors: the library's tensor-core kernel (tcgen05, TMA)
+    for the BF16 and F32 (TF32) stores, cuBLAS DGEMM for F64; beside it the
+    same BF16 GEMM through cuBLAS (torch.matmul) and the K-split sweep."""
     import torch
-    A = capi.DeviceMatrix.generate("DENSE", "cqmat", n, n, 16, Q_HEADLINE, 0, stores=capi.STORE_F64 | capi.STORE_BF16)
-    res = {}
-    for name, store, tdt in (("f64", capi.F64, torch.float64), ("bf16", capi.BF16, torch.float32)):
-        X = torch.rand((k, n), dtype=tdt, device="cuda")
-        Y = torch.empty((k, n), dtype=tdt, device="cuda")
-        s = torch.cuda.current_stream().cuda_stream
+    peak, _ = peaks()
+    A = capi.DeviceMatrix.generate("DENSE", "cqmat", n, n, 16, Q_HEADLINE, 0,
+                                   stores=capi.STORE_F64 | capi.STORE_F32 | capi.STORE_BF16)
+    res = {"n": n, "k": k}
+    s = torch.cuda.current_stream().cuda_stream
+
+    def timed(fn, reps=10):
         for _ in range(3):
-            A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s)
+            fn()
+        torch.cuda.synchronize()
         e0, e1 = _events()
         e0.record()
-        for _ in range(5):
-            A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s)
+        for _ in range(reps):
+            fn()
         e1.record()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / 5
-        vb = 8 if store == capi.F64 else 2
-        res[name] = {"ms": round(ms, 3), "TFLOP_s": round(2.0 * n * n * k / ms / 1e9, 1),
-                     "GB_s": round((n * n * vb + 2 * n * k * (8 if store == capi.F64 else 4)) / ms / 1e6, 1)}
+        return e0.elapsed_time(e1) / reps
+
+    for name, store, tdt, vb in (("f64", capi.F64, torch.float64, 8), ("f32_tf32", capi.F32, torch.float32, 4),
+                                 ("bf16", capi.BF16, torch.float32, 2)):
+        X = torch.rand((k, n), dtype=tdt, device="cuda")
+        Y = torch.empty((k, n), dtype=tdt, device="cuda")
+        ms = timed(lambda: A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s), 3 if vb == 8 else 10)
+        algo = n * n * vb + 2 * n * k * (8 if vb == 8 else 4)
+        res[name] = {"ms": round(ms, 4), "TFLOP_s": round(2.0 * n * n * k / ms / 1e9, 1),
+                     "GB_s": round(algo / ms / 1e6, 1), "frac_hbm": round(algo / ms / 1e6 / peak, 3)}
+        if store != capi.F64:
+            sweep = {}
+            for split in (1, 2, 4, 8, 16):
+                A.tune(capi.TUNE_TC_SPLIT, split)
+                sweep[str(split)] = round(timed(lambda: A.dense_spmm(store, k, X.data_ptr(), n, Y.data_ptr(), n, s)), 4)
+            A.tune(capi.TUNE_TC_SPLIT, 0)
+            res[name]["ms_by_k_split"] = sweep
+        del X, Y
+    res["device_status"] = A.device_status()
     A.close()
+    torch.cuda.empty_cache()
+    # the same BF16 GEMM through cuBLAS, for comparison
+    Ab = torch.rand((n, n), device="cuda").to(torch.bfloat16)
+    Xb = torch.rand((n, k), device="cuda").to(torch.bfloat16)
+    ms = timed(lambda: torch.matmul(Ab, Xb))
+    res["cublas_bf16_torch_matmul_ms"] = round(ms, 4)
+    del Ab, Xb
     torch.cuda.empty_cache()
     return res
 
@@ -873,7 +899,8 @@ def main():
     ap.add_argument("--log2n", type=int, default=24, help="headline matrix size 2^log2n (profiling cases)")
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
-    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats", "cfg1"],
+    ap.add_argument("--dense-k", type=int, default=64, help="vectors of the DENSE multi-vector section")
+    ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats", "cfg1", "dense"],
                     default=None,
                     help="only one section of the full report (profiling cases)")
     args = ap.parse_args()
@@ -887,6 +914,9 @@ def main():
         elif args.section == "batching":
             print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22)}),
                   flush=True)
+        elif args.section == "dense":
+            nd = 32768 if args.log2n >= 24 else 1 << (args.log2n - 9)
+            print(json.dumps({"dense": dense_multi(capi, nd, args.dense_k)}), flush=True)
         elif args.section == "cfg1":
             print(json.dumps({"cfg1": cfg1_bench(capi, peaks()[0])}), flush=True)
         elif args.section == "formats":

@@ -182,12 +182,17 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         mixed-precision modes only: TBSLA_PR_REFERENCE
  *                         (page_rank, personalized_page_rank) always sweeps
  *                         the handle itself, so its iteration count follows
- *                         the reference's summation order at every size. */
+ *                         the reference's summation order at every size.
+ *   TBSLA_TUNE_TC_SPLIT   DENSE tensor-core product (tbsla_dense_spmm, F32 /
+ *                         BF16 stores): the number of parts K is split into,
+ *                         1, 2, 4, 8 or 16, or 0 (default) to choose per call
+ *                         from the shape and the SM count. */
 typedef enum {
   TBSLA_TUNE_X_L2_KEEP = 0,
   TBSLA_TUNE_PR_RELABEL = 1,
   TBSLA_TUNE_X_L2_RANGE = 2,
-  TBSLA_TUNE_SHORT_ROWS = 3
+  TBSLA_TUNE_SHORT_ROWS = 3,
+  TBSLA_TUNE_TC_SPLIT = 4
 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);
@@ -240,14 +245,27 @@ tbsla_status_t tbsla_csr_grad_values(const tbsla_matrix_t *A, tbsla_dtype_t type
 tbsla_status_t tbsla_matrix_set_values(tbsla_matrix_t *A, tbsla_dtype_t type, const void *d_values,
                                        void *stream);
 
-/* Y = A X for a DENSE handle and k vectors: X column-major ln_col x k (leading
- * dimension ldx), Y column-major n_row x k (ldy); rows past ln_row give 0.
- * A plain GEMM, done by cuBLAS: FP64 vectors for the F64 store, FP32 for F32
- * and BF16 (the BF16 store runs on the tensor cores with X rounded to BF16,
- * FP32 accumulation).  No reference counterpart (the reference multiplies one
- * vector). */
+/* Y = A X for a DENSE handle and k vectors, each column of Y one
+ * MatrixDENSE::Ax (src/cpp/matrix/MatrixDENSE.cpp:64-73): X column-major
+ * ln_col x k (leading dimension ldx), Y column-major n_row x k (ldy); rows
+ * past ln_row give 0.  FP64 vectors for the F64 store (cuBLAS DGEMM on the
+ * FP64 pipe), FP32 for F32 and BF16, which run on the tensor cores in this
+ * library's own kernel (tcgen05 MMA, operands staged by TMA, FP32
+ * accumulation in TMEM): the F32 store as TF32 with X read as TF32, the BF16
+ * store with X rounded to BF16.  K is split into parts when the row tiles
+ * alone do not fill the GPU (TBSLA_TUNE_TC_SPLIT); the parts are summed in
+ * part order, so results are reproducible.  Rows of A and vectors of X that
+ * do not start on 16-byte boundaries are copied to padded buffers first
+ * (ln_col a multiple of 8 for BF16, 4 for F32, and such an ldx avoid it).
+ * Work buffers come from the stream-ordered allocator (cudaMallocAsync).
+ * A kernel whose bounded wait gave up raises the handle's device status
+ * (tbsla_matrix_device_status). */
 tbsla_status_t tbsla_dense_spmm(const tbsla_matrix_t *A, tbsla_dtype_t store, int k, const void *d_X,
                                 int64_t ldx, void *d_Y, int64_t ldy, void *stream);
+/* Synchronises the handle's device and returns in *status, then clears, the
+ * handle's device status: nonzero when one of its kernels gave up a bounded
+ * wait (its results are then not valid).  No reference counterpart. */
+tbsla_status_t tbsla_matrix_device_status(const tbsla_matrix_t *A, int *status);
 
 /* Y = A X for k vectors of a CSR or COO / SCOO handle, X and Y row-major
  * (vector index fastest: X[j*ldx + c] is entry j of vector c, ldx, ldy >= k;

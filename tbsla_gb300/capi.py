@@ -21,7 +21,7 @@ FMT_NAME = {v: k for k, v in FMT.items()}
 F64, F32, BF16 = 0, 1, 2
 STORE_F64, STORE_F32, STORE_BF16 = 1, 2, 4
 PR_REFERENCE, PR_DANGLING, PR_TELEPORT = 0, 1, 2
-TUNE_X_L2_KEEP, TUNE_PR_RELABEL, TUNE_X_L2_RANGE, TUNE_SHORT_ROWS = 0, 1, 2, 3
+TUNE_X_L2_KEEP, TUNE_PR_RELABEL, TUNE_X_L2_RANGE, TUNE_SHORT_ROWS, TUNE_TC_SPLIT = 0, 1, 2, 3, 4
 GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2, "cqmat_baseline": 3}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -82,6 +82,7 @@ def lib() -> C.CDLL:
         "tbsla_matrix_set_variant": ([P, C.c_int], st),
         "tbsla_matrix_tune": ([P, C.c_int, C.c_double], st),
         "tbsla_matrix_info": ([P, C.POINTER(MatrixInfo)], st),
+        "tbsla_matrix_device_status": ([P, C.POINTER(C.c_int)], st),
         "tbsla_spmv": ([P, _vp, _vp, C.c_int, _vp], st),
         "tbsla_spmv_ex": ([P, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp], st),
         "tbsla_spmv_host": ([P, _vp, C.c_int64, _vp, C.c_int64, C.c_int], st),
@@ -414,6 +415,13 @@ class DeviceMatrix:
 
     def dense_spmm(self, store: int, k: int, d_X: int, ldx: int, d_Y: int, ldy: int, stream=None):
         check(lib().tbsla_dense_spmm(self.h, store, k, d_X, ldx, d_Y, ldy, stream))
+
+    def device_status(self) -> int:
+        """Nonzero when a kernel of this handle gave up a bounded wait
+        (synchronises the device; clears the status)."""
+        st = C.c_int(0)
+        check(lib().tbsla_matrix_device_status(self.h, C.byref(st)))
+        return st.value
 
     def spmm(self, store: int, k: int, d_X: int, ldx: int, d_Y: int, ldy: int, stream=None):
         """Y = A X for k row-major vectors (CSR, COO, SCOO)."""

@@ -132,6 +132,7 @@ struct tbsla_matrix {
   float *tile_head_val32 = nullptr;  // FP32-accumulating variants
   float *tile_tail_val32 = nullptr;
   int *d_err = nullptr;              // set by a kernel whose bounded wait gave up
+  int tc_split = 0;                  // DENSE tensor-core product: K splits (0: chosen per call)
 
   // PageRank workspace built on first use (pagerank.cu)
   void *pr_work = nullptr;

@@ -743,6 +743,11 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
     A->short_mode = (int)value;
     if (A->pr_relabel) A->pr_relabel->short_mode = (int)value;
     return TBSLA_OK;
+  case TBSLA_TUNE_TC_SPLIT:
+    TB_CHECK(value == 0.0 || value == 1.0 || value == 2.0 || value == 4.0 || value == 8.0 || value == 16.0,
+             "tensor-core K split %g not 0, 1, 2, 4, 8 or 16", value);
+    A->tc_split = (int)value;
+    return TBSLA_OK;
   case TBSLA_TUNE_X_L2_RANGE:
     TB_CHECK(value == 0.0 || value == 1.0, "x L2 range mode %g not 0 or 1", value);
     A->x_keep_range = (int)value;

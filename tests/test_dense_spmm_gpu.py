@@ -1,34 +1,103 @@
-"""Multi-vector DENSE product (tbsla_dense_spmm, cuBLAS GEMM) against numpy:
-FP64 within the FP64 bound of the product tests, FP32 within 1e-5 and the
-BF16 store (tensor cores, inputs rounded to BF16) within 1e-2 of
-sum |a_ij x_jc|; leading dimensions larger than the shapes; rows past ln_row
-give 0."""
+"""Multi-vector DENSE product (tbsla_dense_spmm) against the oracle's k
+DENSE products (MatrixDENSE::Ax, src/cpp/matrix/MatrixDENSE.cpp:64-73).
+
+The F32 and BF16 stores run on the tensor cores (the library's tcgen05
+kernel): TF32 within 4e-3 and BF16 within 1.2e-2 of sum_j |a_ij x_jc| (the
+operands' rounding: 2^-10 / 2^-8 relative each, plus FP32 accumulation); the
+BF16 result also against the FP64 product of the rounded operands within
+K * 2^-23 of the same sum (accumulation error only).  F64 (FP64 pipe) within
+the FP64 bound of the product tests.  Shapes cover row tiles cut by the
+matrix edge, K not a multiple of the 128-byte stage, unaligned leading
+dimensions (padded copies), one to several vector panels, rows past ln_row
+(zero), every K split, and the same bits on a repeated call.
+"""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
+SHAPES = [
+    # n_row, ln_row, ln_col, k, ldx, ldy
+    (800, 700, 500, 16, 512, 808),
+    (1000, 1000, 1024, 64, 1024, 1000),
+    (300, 257, 333, 5, 340, 300),
+    (256, 256, 2048, 100, 2050, 260),
+    (130, 130, 4096, 300, 4096, 130),
+    (128, 128, 64, 1, 64, 128),
+]
 
-def test_dense_multi_vector(gpu):
-    rng = np.random.default_rng(6)
-    n_row, ln_row, ln_col, k, ldx, ldy = 800, 700, 500, 16, 512, 808
+
+def bf16_round(a):
+    """Round-to-nearest-even to BF16 (as the device's stores and X copy do)."""
+    return torch.from_numpy(np.ascontiguousarray(a)).to(torch.bfloat16).double().numpy()
+
+
+def oracle_products(orc, a, x, n_row):
+    """Column c = the oracle's MatrixDENSE product of vector c (rows past
+    ln_row are 0)."""
+    ln_row, ln_col = a.shape
+    geom = [n_row, ln_col, ln_row, ln_col, 0, 0, 0, 0, 1, 1, 0]
+    m = orc.from_layout("DENSE", geom, a.size, a.ravel(), np.zeros(0, np.int32), np.zeros(0, np.int32))
+    return np.stack([m.spmv(x[:, c]) for c in range(x.shape[1])], axis=1)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_dense_multi_vector_against_oracle(gpu, orc, shape):
+    n_row, ln_row, ln_col, k, ldx, ldy = shape
+    rng = np.random.default_rng(hash(shape) % 2**32)
     a = rng.uniform(-1, 1, (ln_row, ln_col))
     A = gpu.DeviceMatrix.dense(n_row, ln_col, ln_row, ln_col, a.ravel(),
                                stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
     x = rng.uniform(-1, 1, (ln_col, k))
-    ref = np.zeros((n_row, k))
-    ref[:ln_row] = a @ x
-    bound = np.zeros((n_row, k))
-    bound[:ln_row] = np.abs(a) @ np.abs(x)
+    ref = oracle_products(orc, a, x, n_row)
+    bound = oracle_products(orc, np.abs(a), np.abs(x), n_row)
+    ar, xr = bf16_round(a), bf16_round(x.astype(np.float32))
+    ref_r = oracle_products(orc, ar, xr, n_row)
     dev = torch.device("cuda")
-    for store, tdt, tol in ((gpu.F64, torch.float64, 1e-12), (gpu.F32, torch.float32, 1e-5),
-                            (gpu.BF16, torch.float32, 1e-2)):
-        X = torch.zeros((k, ldx), dtype=tdt, device=dev)  # column c at X[c, :]
+    for store, tdt, tol in ((gpu.F64, torch.float64, 1e-12), (gpu.F32, torch.float32, 4e-3),
+                            (gpu.BF16, torch.float32, 1.2e-2)):
+        X = torch.zeros((k, ldx), dtype=tdt, device=dev)  # vector c at X[c, :ln_col]
         X[:, :ln_col] = torch.from_numpy(x.T.copy()).to(dev, tdt)
-        Y = torch.full((k, ldy), float("nan"), dtype=tdt, device=dev)
-        A.dense_spmm(store, k, X.data_ptr(), ldx, Y.data_ptr(), ldy)
+        splits = (0,) if store == gpu.F64 else (0, 1, 2, 4)
+        for split in splits:
+            A.tune(gpu.TUNE_TC_SPLIT, split)
+            outs = []
+            for _ in range(2):
+                Y = torch.full((k, ldy), float("nan"), dtype=tdt, device=dev)
+                A.dense_spmm(store, k, X.data_ptr(), ldx, Y.data_ptr(), ldy)
+                torch.cuda.synchronize()
+                outs.append(Y[:, :n_row].double().cpu().numpy().T)
+            y = outs[0]
+            assert np.array_equal(outs[0], outs[1]), (store, split, "results differ between two calls")
+            err = np.abs(y - ref)
+            assert np.all(err <= tol * bound + 1e-300), (store, split, float((err / (bound + 1e-300)).max()))
+            assert np.all(y[ln_row:] == 0)
+            if store == gpu.BF16:
+                err_r = np.abs(y - ref_r)
+                assert np.all(err_r <= ln_col * 2.0 ** -23 * bound + 1e-300), (split, float(err_r.max()))
+            # the columns past n_row of Y are not written
+            Yfull = Y.cpu()
+            if ldy > n_row:
+                assert torch.isnan(Yfull[:, n_row:]).all()
+    assert A.device_status() == 0
+
+
+def test_dense_multi_vector_splits_agree(gpu):
+    """Every K split gives results within FP32 summation-order bounds of the
+    others; the product is deterministic for a given split."""
+    rng = np.random.default_rng(3)
+    n, k = 512, 64
+    a = rng.uniform(0, 1, (n, 8192))
+    A = gpu.DeviceMatrix.dense(n, 8192, n, 8192, a.ravel(), stores=gpu.STORE_BF16 | gpu.STORE_F64)
+    X = torch.rand((k, 8192), dtype=torch.float32, device="cuda")
+    ys = {}
+    for split in (1, 2, 4, 8, 16):
+        A.tune(gpu.TUNE_TC_SPLIT, split)
+        Y = torch.empty((k, n), dtype=torch.float32, device="cuda")
+        A.dense_spmm(gpu.BF16, k, X.data_ptr(), 8192, Y.data_ptr(), n)
         torch.cuda.synchronize()
-        y = Y[:, :n_row].double().cpu().numpy().T
-        assert np.all(np.abs(y - ref) <= tol * bound + 1e-300), store
-        assert np.all(y[ln_row:] == 0)
+        ys[split] = Y.double().cpu().numpy()
+    for split, y in ys.items():
+        np.testing.assert_allclose(y, ys[1], rtol=1e-5, err_msg=f"split {split}")
+    assert A.device_status() == 0

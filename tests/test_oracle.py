@@ -143,6 +143,39 @@ def test_spmv_iota_and_page_rank_match_golden(orc, golden):
         assert it == rec["ppr"]["it"] and [repr(float(v)) for v in b] == rec["ppr"]["b"]
 
 
+def test_exact_sum_page_rank_against_golden_and_oracle(orc, golden):
+    """The exact-sum restatement of Matrix::page_rank / personalized_page_rank
+    (oracle.page_rank_exact_sums) against the reference's golden vectors
+    (small: the sums' order is immaterial there) and, on an R-MAT graph of
+    2^16 vertices, against the reference-faithful oracle: same iteration
+    counts, vectors within the reference's own summation error (n-1) u."""
+    from oracle.oracle import page_rank_exact_sums
+    for rec in golden["page_rank"]:
+        nr, nc, c = rec["shape"]
+        if nr != nc or rec["format"] != "CSR":
+            continue
+        a = orc.fill_cqmat_stochastic("CSR", nr, nc, c, rec["q"], rec["seed"]).arrays
+        b, it = page_rank_exact_sums(a.rowptr, a.colidx, a.values, 1e-10, 0.85, 500)
+        ref = np.array([float(v) for v in rec["tight"]["b"]])
+        assert it == rec["tight"]["it"] and np.abs(b - ref).sum() < 1e-14
+        p, it = page_rank_exact_sums(a.rowptr, a.colidx, a.values, 0.85, 0.01, 10, [1, 3])
+        ref = np.array([float(v) for v in rec["ppr"]["b"]])
+        assert it == rec["ppr"]["it"] and np.abs(p - ref).sum() < 1e-14
+    scale = 16
+    n = 1 << scale
+    src, dst = orc.rmat_edges(scale, 16 << scale, seed=3)
+    key = np.unique((dst.astype(np.int64) << scale) | src.astype(np.int64))
+    d, sc = (key >> scale).astype(np.int32), (key & (n - 1)).astype(np.int32)
+    rp = np.zeros(n + 1, np.int64)
+    np.add.at(rp, d + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    va = 1.0 / np.bincount(sc, minlength=n)[sc]
+    o = orc.from_arrays("CSR", n, n, va, rp, sc)
+    bo, it = o.page_rank(1e-9, 0.85, 500)
+    be, ite = page_rank_exact_sums(rp, sc, va, 1e-9, 0.85, 500)
+    assert it == ite and np.abs(be - bo).sum() <= n * 2.0 ** -53
+
+
 def test_cfg1_matches_golden(orc, golden):
     g = golden["cfg1"]
     m = orc.fill_cqmat("CSR", 100000, 100000, 10, 0.1, 0)

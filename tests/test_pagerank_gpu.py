@@ -139,24 +139,34 @@ def test_reference_mode_large_skewed_against_oracle(gpu, orc, relabel):
     non-banded R-MAT graph of 2^20 vertices, where the dangling mode takes the
     degree-relabelled copy: the reference mode sweeps the handle itself (with
     the automatic rule and with relabelling forced), so it stops after the
-    oracle's iteration count with the oracle's vector to 1e-12."""
+    oracle's iteration count.  Its vector is within 1e-12 of the reference's
+    iteration with correctly rounded sums (page_rank_exact_sums); the
+    reference's own left-to-right sums of 2^20 positive values move its
+    vector by up to (n-1) u, 1.5e-11 here, and the GPU stays within that
+    bound of the reference-faithful oracle."""
+    from oracle.oracle import page_rank_exact_sums
     scale = 20
     m = 16 << scale
     A = gpu.DeviceMatrix.rmat_pagerank(scale, m, seed=3)
     A.tune(gpu.TUNE_PR_RELABEL, relabel)
     rp, ci, va, _ = rmat_csr_oracle(orc, scale, m, 3)
     n = 1 << scale
+    sum_bound = 4 * n * 2.0 ** -53
     o = orc.from_arrays("CSR", n, n, va, rp, ci)
     for eps in (1e-9, 1e-6):
         b, r = A.pagerank_host(beta=0.85, tol=eps, max_iter=500, mode=gpu.PR_REFERENCE)
         bo, it = o.page_rank(eps, 0.85, 500, threads=1)
-        assert r.iterations == it, (eps, r.iterations, it)
-        assert np.abs(b - bo).sum() <= 1e-12, (eps, np.abs(b - bo).sum())
+        be, ite = page_rank_exact_sums(rp, ci, va, eps, 0.85, 500)
+        assert r.iterations == it == ite, (eps, r.iterations, it, ite)
+        assert np.abs(b - be).sum() <= 1e-12, (eps, np.abs(b - be).sum())
+        assert np.abs(b - bo).sum() <= sum_bound, (eps, np.abs(b - bo).sum())
     nodes = [0, 7, 7, n - 1, 12345]
     p, r = A.personalized_pagerank_host(nodes, beta=0.85, tol=1e-9, max_iter=500)
     po, it = o.personalized_page_rank(1e-9, 0.85, 500, nodes, threads=1)
-    assert r.iterations == it, (r.iterations, it)
-    assert np.abs(p - po).sum() <= 1e-12, np.abs(p - po).sum()
+    pe, ite = page_rank_exact_sums(rp, ci, va, 1e-9, 0.85, 500, nodes)
+    assert r.iterations == it == ite, (r.iterations, it, ite)
+    assert np.abs(p - pe).sum() <= 1e-12, np.abs(p - pe).sum()
+    assert np.abs(p - po).sum() <= sum_bound, np.abs(p - po).sum()
 
 
 def test_pagerank_argument_checks(gpu):
