@@ -29,8 +29,12 @@ SHAPES = [
 
 
 def bf16_round(a):
-    """Round-to-nearest-even to BF16 (as the device's stores and X copy do)."""
-    return torch.from_numpy(np.ascontiguousarray(a)).to(torch.bfloat16).double().numpy()
+    """Round-to-nearest-even of each value to BF16 (8 significant bits) in one
+    step, as the device's BF16 store (from FP64) and X copy (from FP32) do:
+    the significand scaled to 8 bits, rounded half to even, scaled back (all
+    exact in FP64)."""
+    m, e = np.frexp(np.asarray(a, np.float64))
+    return np.ldexp(np.rint(m * 256.0) / 256.0, e)
 
 
 def oracle_products(orc, a, x, n_row):
@@ -84,20 +88,22 @@ def test_dense_multi_vector_against_oracle(gpu, orc, shape):
 
 
 def test_dense_multi_vector_splits_agree(gpu):
-    """Every K split gives results within FP32 summation-order bounds of the
-    others; the product is deterministic for a given split."""
+    """Every K split (1 to 16 parts of an 8192-long sum) is within the FP32
+    accumulation bound K * 2^-23 * sum |a x| of the FP64 product of the
+    BF16-rounded operands."""
     rng = np.random.default_rng(3)
-    n, k = 512, 64
-    a = rng.uniform(0, 1, (n, 8192))
-    A = gpu.DeviceMatrix.dense(n, 8192, n, 8192, a.ravel(), stores=gpu.STORE_BF16 | gpu.STORE_F64)
-    X = torch.rand((k, 8192), dtype=torch.float32, device="cuda")
-    ys = {}
+    n, K, k = 512, 8192, 64
+    a = rng.uniform(0, 1, (n, K))
+    A = gpu.DeviceMatrix.dense(n, K, n, K, a.ravel(), stores=gpu.STORE_BF16 | gpu.STORE_F64)
+    x = rng.uniform(0, 1, (k, K)).astype(np.float32)
+    X = torch.from_numpy(x).cuda()
+    ref = bf16_round(a) @ bf16_round(x).T  # n x k, all terms positive: sum |a x| = ref
     for split in (1, 2, 4, 8, 16):
         A.tune(gpu.TUNE_TC_SPLIT, split)
         Y = torch.empty((k, n), dtype=torch.float32, device="cuda")
-        A.dense_spmm(gpu.BF16, k, X.data_ptr(), 8192, Y.data_ptr(), n)
+        A.dense_spmm(gpu.BF16, k, X.data_ptr(), K, Y.data_ptr(), n)
         torch.cuda.synchronize()
-        ys[split] = Y.double().cpu().numpy()
-    for split, y in ys.items():
-        np.testing.assert_allclose(y, ys[1], rtol=1e-5, err_msg=f"split {split}")
+        y = Y.double().cpu().numpy().T
+        err = float((np.abs(y - ref) / ref).max())
+        assert err <= K * 2.0 ** -23, (split, err)
     assert A.device_status() == 0
