@@ -77,6 +77,11 @@ const char *tbsla_status_string(tbsla_status_t s);
 int tbsla_version(void);
 /* device the library uses for new handles (default: current device) */
 tbsla_status_t tbsla_set_device(int device);
+/* The device's name (into name, name_len bytes, NUL-terminated), its
+ * theoretical HBM rate in GB/s (memory clock x bus width, double data rate)
+ * and its SM count; NULL pointers skip a field.  For reports such as the
+ * driver programs' roofline fraction. */
+tbsla_status_t tbsla_device_describe(int device, char *name, int name_len, double *hbm_gbs, int *sms);
 /* The current device's L2 fetch granularity for this process (the CUDA
  * context limit cudaLimitMaxL2FetchGranularity; 32, 64 or 128 bytes): how
  * much a missing load brings from DRAM.  The kernels ask for 256-byte
@@ -443,6 +448,20 @@ tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_p
                                  const int *nodes, const int *offsets, int tile, double *d_out, int *iterations,
                                  double *residuals, void *stream);
 
+/* As tbsla_ppr_batched with p->precision = TBSLA_F32, corrected to FP64
+ * accuracy (the F64 and F32 value stores are needed): the FP32 batched solve
+ * (stopped at max(p->tol, 1e-6)), then rounds of r = G(x) - x by one FP64
+ * sweep of every vector; when every ||r_c||_1 < p->tol the result is G(x),
+ * else the FP32 batched correction solve e = beta A e + beta (d.e) v_c + r_c
+ * (from e = r_c, to ||e_j+1 - e_j||_1 < 1e-3 ||r_c||_1) and x += e, at most
+ * 8 rounds.  FP64 is used only for the residual sweeps, the L1 norms and the
+ * update.  iterations: FP32 and FP64 sweeps together; residuals: the last
+ * ||r_c||_1.  Allocates 2 n k doubles of work space per call (stream
+ * ordered).  No reference counterpart. */
+tbsla_status_t tbsla_ppr_batched_refined(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                         const int *nodes, const int *offsets, int tile, double *d_out,
+                                         int *iterations, double *residuals, void *stream);
+
 /* Matrix::personalized_page_rank (Matrix.cpp:63-114): as TBSLA_PR_REFERENCE
  * with b0 = 0.25 and the teleport term (1-beta)*sum(b_prev)/n_nodes added only
  * to the listed nodes (a node listed twice counts once but n_nodes is the
@@ -522,6 +541,19 @@ tbsla_status_t tbsla_generate(int format, int gen, int n_row, int n_col, int c, 
  * stores (the matrices tbsla_perf times, src/cpp/apps/tbsla_perf.cpp:111-119). */
 tbsla_status_t tbsla_generate_matrix(int format, int gen, int n_row, int n_col, int c, double q,
                                      unsigned int seed_mult, int stores, tbsla_matrix_t **out);
+
+/* tbsla_generate_matrix built on the device, for the block (pr, pc, NR, NC):
+ * gen 1 (cdiag) for CSR, ELL and DENSE is generated on the device (closed
+ * form per row: the arrays of MatrixCSR / MatrixELL / MatrixDENSE::fill_cdiag,
+ * src/cpp/matrix/MatrixCSR.cpp:234-297, MatrixELL.cpp:192-260,
+ * MatrixDENSE.cpp:137-190, bit for bit); gen 2 (cqmat_stochastic) for CSR,
+ * ELL and DENSE takes fill_cqmat's pattern and the column sums of the global
+ * generator from the host (glibc rand_r draws) and divides on the device
+ * (MatrixCSR.cpp:411-421, MatrixELL.cpp:394-404, MatrixDENSE.cpp:273-286).
+ * Other formats and generators: the host path, whole matrix only. */
+tbsla_status_t tbsla_generate_device(int format, int gen, int n_row, int n_col, int c, double q,
+                                     unsigned int seed_mult, int pr, int pc, int NR, int NC, int stores,
+                                     tbsla_matrix_t **out);
 
 /* R-MAT digraph with 2^scale nodes and m edge draws (Chakrabarti, Zhan,
  * Faloutsos 2004), generated on the device with counter-based draws, as the

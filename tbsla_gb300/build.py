@@ -1,4 +1,5 @@
-"""Builds libtbsla_gb300.so in-tree for sm_103a.
+"""Builds libtbsla_gb300.so in-tree for sm_103a, and the driver programs
+(tbsla_gb300/apps) into tbsla_gb300/bin.
 
 ``python -m tbsla_gb300.build`` or ``tbsla_gb300.build.build()``.  CUDA
 sources go through nvcc with ``-gencode arch=compute_103a,code=sm_103a``, C++
@@ -20,6 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtbsla_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
+APPS = os.path.join(HERE, "apps")
+BIN = os.path.join(HERE, "bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -45,11 +48,36 @@ def _deps() -> list[str]:
                                                                        recursive=True) + [__file__])
 
 
+def apps() -> list[str]:
+    """The driver programs (tbsla_gb300/apps/*.cpp), built into tbsla_gb300/bin."""
+    return sorted(glob.glob(os.path.join(APPS, "*.cpp")))
+
+
+def app_path(name: str) -> str:
+    return os.path.join(BIN, name)
+
+
 def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(d) <= t for d in _deps())
+    if not all(os.path.getmtime(d) <= t for d in _deps()):
+        return False
+    for src in apps():
+        exe = app_path(os.path.splitext(os.path.basename(src))[0])
+        if not os.path.exists(exe) or os.path.getmtime(exe) < max(t, os.path.getmtime(src)):
+            return False
+    return True
+
+
+def _build_app(src: str) -> str:
+    exe = app_path(os.path.splitext(os.path.basename(src))[0])
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", f"-I{INCLUDE}", f"-I{APPS}", src,
+           f"-L{HERE}", "-ltbsla_gb300", "-Wl,-rpath,$ORIGIN/..", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return exe
 
 
 def _obj(src: str) -> str:
@@ -85,8 +113,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    os.makedirs(BIN, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=max(2, len(apps()))) as ex:
+        list(ex.map(_build_app, apps()))
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {len(apps())} driver programs in {BIN}")
     return LIB
 
 

@@ -83,6 +83,8 @@ def lib() -> C.CDLL:
         "tbsla_matrix_tune": ([P, C.c_int, C.c_double], st),
         "tbsla_matrix_info": ([P, C.POINTER(MatrixInfo)], st),
         "tbsla_matrix_device_status": ([P, C.POINTER(C.c_int)], st),
+        "tbsla_generate_device": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_int,
+                                   C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)], st),
         "tbsla_spmv": ([P, _vp, _vp, C.c_int, _vp], st),
         "tbsla_spmv_ex": ([P, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp], st),
         "tbsla_spmv_host": ([P, _vp, C.c_int64, _vp, C.c_int64, C.c_int], st),
@@ -126,6 +128,8 @@ def lib() -> C.CDLL:
         "tbsla_batch_spmv_graph": ([_vp, _vp], st),
         "tbsla_batch_destroy": ([_vp], st),
         "tbsla_ppr_batched": ([P, C.POINTER(PageRankParams), C.c_int, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp], st),
+        "tbsla_ppr_batched_refined": ([P, C.POINTER(PageRankParams), C.c_int, _vp, _vp, C.c_int, _vp, _vp, _vp,
+                                       _vp], st),
         "tbsla_autotune_spmv": ([P, C.c_int, C.POINTER(AutotuneResult)], st),
         "tbsla_matrix_read_file": ([C.c_char_p, C.c_int, C.c_int64, C.POINTER(P)], st),
         "tbsla_matrix_read_mm": ([C.c_char_p, C.c_int, C.POINTER(P)], st),
@@ -282,6 +286,15 @@ class DeviceMatrix:
         """One pass: generate on the host and upload (tbsla_generate_matrix)."""
         h = _vp()
         check(lib().tbsla_generate_matrix(FMT[fmt], GEN[gen], n_row, n_col, c, q, seed_mult, stores, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def generate_device(cls, fmt: str, gen: str, n_row: int, n_col: int, c: int, q: float = 0.0,
+                        seed_mult: int = 1, pr: int = 0, pc: int = 0, NR: int = 1, NC: int = 1, stores=STORE_F64):
+        """Generated on the device where the generator allows (tbsla_generate_device)."""
+        h = _vp()
+        check(lib().tbsla_generate_device(FMT[fmt], GEN[gen], n_row, n_col, c, q, seed_mult, pr, pc, NR, NC, stores,
+                                          C.byref(h)))
         return cls(h)
 
     @classmethod
@@ -531,8 +544,9 @@ class Batch:
 
 
 def ppr_batched(A, seed_sets, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, precision=F64, tile=0,
-                stream=None, check_every=0):
-    """k personalized PageRank vectors of A solved together; returns (iterations, residuals)."""
+                stream=None, check_every=0, refined=False):
+    """k personalized PageRank vectors of A solved together; returns (iterations, residuals).
+    refined: FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined)."""
     k = len(seed_sets)
     offsets = np.zeros(k + 1, np.int32)
     offsets[1:] = np.cumsum([len(s) for s in seed_sets])
@@ -540,6 +554,6 @@ def ppr_batched(A, seed_sets, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, 
     its = np.zeros(k, np.int32)
     res = np.zeros(k, np.float64)
     p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, precision, check_every)
-    check(lib().tbsla_ppr_batched(A.h, C.byref(p), k, _ptr(nodes), _ptr(offsets), tile, d_out, _ptr(its),
-                                  _ptr(res), stream))
+    fn = lib().tbsla_ppr_batched_refined if refined else lib().tbsla_ppr_batched
+    check(fn(A.h, C.byref(p), k, _ptr(nodes), _ptr(offsets), tile, d_out, _ptr(its), _ptr(res), stream))
     return its, res

@@ -61,6 +61,8 @@ struct TcParams {
   int64_t ld_out;       // distance between vectors in out
   int64_t split_stride; // distance between parts in out
   int *err;             // raised when a bounded wait gave up
+  int a_early;          // A is not written by the stream's previous kernels:
+                        // its first stages load before the dependency wait
 };
 
 template <int N> struct TcShape {
@@ -122,13 +124,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // the vector panel
     const uint64_t pol_a = tc::policy_evict_first(), pol_x = tc::policy_evict_last();
     constexpr int kElems = kRowBytes / (Fmt == tc::kFmtBF16 ? 2 : 4);
+    // A of the first stages may load while the kernel that writes X (or any
+    // earlier kernel of the stream) finishes; X only after the dependency wait
+    const int pre = p.a_early ? min(ST, nkb) : 0;
+    for (int i = 0; i < pre; ++i) {
+      tc::mbar_arrive_expect_tx(full + i, S::kA + S::kB);
+      tc::tma_load_2d(sa + i * S::kA, &map_a, full + i, (kb0 + i) * kElems, m0, pol_a);
+    }
+    tc::grid_dependency_wait();
     int issued = 0;
     for (int i = 0; i < nkb; ++i) {
       const int s = i % ST;
-      if (i >= ST && !tc::mbar_wait(empty + s, ((i / ST) - 1) & 1, abort)) break;
-      tc::mbar_arrive_expect_tx(full + s, S::kA + S::kB);
       const int kx = (kb0 + i) * kElems;
-      tc::tma_load_2d(sa + s * S::kA, &map_a, full + s, kx, m0, pol_a);
+      if (i >= pre) {
+        if (i >= ST && !tc::mbar_wait(empty + s, ((i / ST) - 1) & 1, abort)) break;
+        tc::mbar_arrive_expect_tx(full + s, S::kA + S::kB);
+        tc::tma_load_2d(sa + s * S::kA, &map_a, full + s, kx, m0, pol_a);
+      }
       tc::tma_load_2d(sx + s * S::kB, &map_x, full + s, kx, vec0, pol_x);
       ++issued;
     }
@@ -154,6 +166,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int q = warp & 3;
     const bool ok = tc::mbar_wait(done, 0, abort, true);
     tc::tc_fence_after_sync();
+    tc::grid_dependency_wait();  // the stream's earlier kernels are done with Y
     const int go = __shfl_sync(0xffffffffu, (ok && !*abort) ? 1 : 0, 0);
     if (go) {
       const int row = m0 + q * 32 + lane;
@@ -193,13 +206,28 @@ __global__ void split_sum_kernel(const float *__restrict__ P, int parts, int M, 
   }
 }
 
-// X (FP32 column-major, ldx) rounded to BF16, vector c at out + c * ldo
+// X (FP32 column-major, ldx) rounded to BF16, vector c at out + c * ldo:
+// blockIdx.y walks the vectors, x four entries per thread (one 16-byte load
+// and one 8-byte store when both vectors start on such boundaries).  Lets the
+// next kernel launch at once (it waits for this one before reading X).
 __global__ void x_to_bf16_kernel(const float *__restrict__ x, int rows, int k, int64_t ldx,
-                                 __nv_bfloat16 *__restrict__ out, int64_t ldo) {
-  const int64_t total = (int64_t)rows * k;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = t / rows, r = t % rows;
-    out[c * ldo + r] = __float2bfloat16_rn(x[c * ldx + r]);
+                                 __nv_bfloat16 *__restrict__ out, int64_t ldo, int vec4) {
+  tc::grid_launch_dependents();
+  for (int c = blockIdx.y; c < k; c += gridDim.y) {
+    const float *xc = x + (int64_t)c * ldx;
+    __nv_bfloat16 *oc = out + (int64_t)c * ldo;
+    for (int r = 4 * (blockIdx.x * blockDim.x + threadIdx.x); r < rows; r += 4 * gridDim.x * blockDim.x) {
+      if (vec4 && r + 4 <= rows) {
+        const float4 v = *reinterpret_cast<const float4 *>(xc + r);
+        __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+        uint2 w;
+        w.x = *reinterpret_cast<uint32_t *>(&lo);
+        w.y = *reinterpret_cast<uint32_t *>(&hi);
+        *reinterpret_cast<uint2 *>(oc + r) = w;
+      } else {
+        for (int j = r; j < min(r + 4, rows); ++j) oc[j] = __float2bfloat16_rn(xc[j]);
+      }
+    }
   }
 }
 
@@ -240,8 +268,20 @@ tbsla_status_t launch_tc(const CUtensorMap &ma, const CUtensorMap &mx, const TcP
         cudaFuncSetAttribute(dense_tc_kernel<N, Fmt>, cudaFuncAttributeMaxDynamicSharedMemorySize, Sh::kSmem);
   });
   TB_CUDA(attr_err[Fmt == tc::kFmtBF16 ? 0 : 1]);
-  dense_tc_kernel<N, Fmt><<<dim3(m_tiles, parts, panels), kTcThreads, Sh::kSmem, s>>>(ma, mx, p);
-  TB_CUDA(cudaGetLastError());
+  // programmatic dependent launch: the kernel may start while the stream's
+  // previous kernel finishes; it waits for it (griddepcontrol.wait) before
+  // loading X or storing Y
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(m_tiles, parts, panels);
+  cfg.blockDim = dim3(kTcThreads);
+  cfg.dynamicSmemBytes = Sh::kSmem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TB_CUDA(cudaLaunchKernelEx(&cfg, dense_tc_kernel<N, Fmt>, ma, mx, p));
   return TBSLA_OK;
 }
 
@@ -257,13 +297,14 @@ tbsla_status_t launch_tc_n(int n_pad, const CUtensorMap &ma, const CUtensorMap &
   }
 }
 
-// K parts: double while the CTAs of the launch stay below four per slot of
-// the GPU (two CTAs per SM up to 64 vectors, one above) and every part keeps
-// at least 16 K blocks
-int choose_parts(int m_tiles, int panels, int kb_total, int n_pad, int sms) {
-  const int slots = sms * (n_pad <= 64 ? 2 : 1);
+// K parts: doubled only while the row tiles and panels leave SMs idle and
+// every part keeps at least 16 K blocks.  A split costs a pass over the
+// parts' partial sums; with every SM holding a tile the stages already keep
+// HBM busy (n = 32768, k = 64, BF16: 0.350 ms whole, 0.358 / 0.371 / 0.388 ms
+// in 2 / 4 / 8 parts)
+int choose_parts(int m_tiles, int panels, int kb_total, int sms) {
   int parts = 1;
-  while ((int64_t)m_tiles * panels * parts < 4LL * slots && kb_total / (parts * 2) >= 16 && parts < 16) parts *= 2;
+  while ((int64_t)m_tiles * panels * parts < sms && kb_total / (parts * 2) >= 16 && parts < 16) parts *= 2;
   return parts;
 }
 
@@ -304,11 +345,15 @@ tbsla_status_t dense_spmm_tc(tbsla_matrix *A, bool bf16, int k, const float *X, 
   if (bf16 || (ldx % align) != 0 || (reinterpret_cast<uintptr_t>(X) & 15) != 0) {
     ldxe = (K + align - 1) / align * align;
     TB_CUDA(cudaMallocAsync(&x_buf, (size_t)k * ldxe * es, s));
-    if (bf16)
-      x_to_bf16_kernel<<<152 * 8, 256, 0, s>>>(X, K, k, ldx, static_cast<__nv_bfloat16 *>(x_buf), ldxe);
-    else
+    if (bf16) {
+      const int vec4 = (ldx % 4) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+      const int gx = std::max(1, std::min((K + 1023) / 1024, 64));
+      x_to_bf16_kernel<<<dim3(gx, std::min(k, 65535)), 256, 0, s>>>(X, K, k, ldx,
+                                                                    static_cast<__nv_bfloat16 *>(x_buf), ldxe, vec4);
+    } else {
       pad_rows_kernel<<<152 * 8, 256, 0, s>>>(reinterpret_cast<const uint8_t *>(X), k, (int64_t)K * 4, ldx * 4,
                                                static_cast<uint8_t *>(x_buf), ldxe * 4);
+    }
     x = x_buf;
   }
   const int n_pad = k <= 16 ? 16 : k <= 32 ? 32 : k <= 64 ? 64 : k <= 128 ? 128 : 256;
@@ -317,7 +362,7 @@ tbsla_status_t dense_spmm_tc(tbsla_matrix *A, bool bf16, int k, const float *X, 
   const int kb_total = (int)(((int64_t)K * es + kRowBytes - 1) / kRowBytes);
   int sms = 0;
   TB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, A->device));
-  int parts = A->tc_split > 0 ? A->tc_split : choose_parts(m_tiles, panels, kb_total, n_pad, sms);
+  int parts = A->tc_split > 0 ? A->tc_split : choose_parts(m_tiles, panels, kb_total, sms);
   parts = std::max(1, std::min(parts, kb_total));
   const int kb_per = (kb_total + parts - 1) / parts;
   parts = (kb_total + kb_per - 1) / kb_per;  // every part holds at least one K block
@@ -330,6 +375,7 @@ tbsla_status_t dense_spmm_tc(tbsla_matrix *A, bool bf16, int k, const float *X, 
   p.kb_total = kb_total;
   p.kb_per_split = kb_per;
   p.err = A->d_err;
+  p.a_early = a_pad == nullptr;  // the handle's own store: written at creation only
   if (parts == 1) {
     p.out = Y;
     p.ld_out = ldy;

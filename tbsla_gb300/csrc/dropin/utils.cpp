@@ -1,11 +1,17 @@
 // dropin/utils.cpp -- TBSLA's utility functions (src/cpp/utils/vector.cpp,
-// range.cpp, csr.cpp, values_generation.cpp) for the drop-in headers.
+// range.cpp, csr.cpp, values_generation.cpp, InputParser.cpp, split.cpp,
+// cpuset_to_cstr.cpp) for the drop-in headers.
 #include <algorithm>
 #include <cmath>
 #include <iomanip>
 
+#include <string>
+
+#include <tbsla/cpp/utils/InputParser.hpp>
+#include <tbsla/cpp/utils/cpuset_to_cstr.hpp>
 #include <tbsla/cpp/utils/csr.hpp>
 #include <tbsla/cpp/utils/range.hpp>
+#include <tbsla/cpp/utils/split.hpp>
 #include <tbsla/cpp/utils/values_generation.hpp>
 #include <tbsla/cpp/utils/vector.hpp>
 
@@ -135,3 +141,63 @@ std::vector<double> cqmat_sum_columns(std::size_t nr, std::size_t nc, std::size_
 }
 
 }}}  // namespace tbsla::utils::values_generation
+
+// ------------------------------------------------ driver-program utilities
+// InputParser (src/cpp/utils/InputParser.cpp:4-21)
+InputParser::InputParser(int &argc, char **argv) {
+  for (int i = 1; i < argc; ++i) params.emplace_back(argv[i]);
+}
+
+std::string InputParser::get_opt(const std::string &option, const std::string default_opt) const {
+  for (std::size_t i = 0; i < params.size(); ++i)
+    if (params[i] == option) return i + 1 < params.size() ? params[i + 1] : default_opt;
+  return default_opt;
+}
+
+bool InputParser::has_opt(const std::string &option) const {
+  return std::find(params.begin(), params.end(), option) != params.end();
+}
+
+namespace tbsla { namespace utils { namespace io {
+
+// the non-empty pieces of str between occurrences of delim (an empty delim
+// leaves str whole)
+std::vector<std::string> split(const std::string &str, const std::string &delim) {
+  std::vector<std::string> out;
+  if (delim.empty()) {
+    if (!str.empty()) out.push_back(str);
+    return out;
+  }
+  std::size_t start = 0;
+  while (start <= str.size()) {
+    const std::size_t hit = str.find(delim, start);
+    const std::size_t end = hit == std::string::npos ? str.size() : hit;
+    if (end > start) out.push_back(str.substr(start, end - start));
+    if (hit == std::string::npos) break;
+    start = hit + delim.size();
+  }
+  return out;
+}
+
+}}}  // namespace tbsla::utils::io
+
+namespace tbsla { namespace cpp { namespace utils {
+
+char *cpuset_to_cstr(cpu_set_t *mask, char *str) {
+  std::string out;
+  for (int i = 0; i < CPU_SETSIZE; ++i) {
+    if (!CPU_ISSET(i, mask)) continue;
+    int j = i;
+    while (j + 1 < CPU_SETSIZE && CPU_ISSET(j + 1, mask)) ++j;
+    if (!out.empty()) out += ',';
+    if (j - i >= 2) out += std::to_string(i) + "-" + std::to_string(j);
+    else if (j == i + 1) out += std::to_string(i) + "," + std::to_string(j);
+    else out += std::to_string(i);
+    i = j;
+  }
+  std::copy(out.begin(), out.end(), str);
+  str[out.size()] = '\0';
+  return str;
+}
+
+}}}  // namespace tbsla::cpp::utils

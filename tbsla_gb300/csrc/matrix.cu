@@ -560,6 +560,25 @@ tbsla_status_t tbsla_set_device(int device) {
   return TBSLA_OK;
 }
 
+tbsla_status_t tbsla_device_describe(int device, char *name, int name_len, double *hbm_gbs, int *sms) {
+  int n = 0;
+  TB_CUDA(cudaGetDeviceCount(&n));
+  TB_CHECK(device >= 0 && device < n, "device %d out of range (%d devices)", device, n);
+  cudaDeviceProp prop{};
+  TB_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (name && name_len > 0) {
+    std::snprintf(name, (size_t)name_len, "%s", prop.name);
+  }
+  if (hbm_gbs) {
+    int khz = 0, bits = 0;
+    TB_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrMemoryClockRate, device));
+    TB_CUDA(cudaDeviceGetAttribute(&bits, cudaDevAttrGlobalMemoryBusWidth, device));
+    *hbm_gbs = 2.0 * khz * 1e3 * (bits / 8.0) / 1e9;  // double data rate
+  }
+  if (sms) *sms = prop.multiProcessorCount;
+  return TBSLA_OK;
+}
+
 tbsla_status_t tbsla_csr_create(int n_row, int n_col, int f_col, int rows, const int *rowptr,
                                 const int *colidx, const double *values, int stores,
                                 tbsla_matrix_t **out) {

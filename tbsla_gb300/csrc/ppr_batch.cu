@@ -24,6 +24,7 @@
 // Large skewed graphs run on the degree-relabelled copy (pr_relabel.cu);
 // seeds are mapped in and the results gathered back to the original labels.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -38,8 +39,9 @@ namespace {
 constexpr int kPprChunk = 512;
 
 struct ColCtl {
-  double add;    // beta * d.x + 1 - beta of the current iterate
+  double add;    // beta * d.x + cst of the current iterate
   double resid;  // last L1 change
+  double tol;    // the column's stopping threshold
   int iter, done;
 };
 struct TileCtl {
@@ -78,14 +80,15 @@ __device__ __forceinline__ void block_columns(double r, double d, double *partia
 template <typename T, int KT>
 __device__ __forceinline__ void ppr_emit(int row, int c, T acc, const T *xo, T *xn, const unsigned *seeds,
                                          const unsigned char *dmask, const ColCtl *col, const double *inv_size,
-                                         double beta, double &r_acc, double &d_acc) {
+                                         double beta, const T *rhs, double &r_acc, double &d_acc) {
   const ColCtl cc = col[c];
   const T old = xo[(size_t)row * KT + c];
   T y;
   if (cc.done) {
     y = old;
   } else {
-    const double t = ((seeds[row] >> c) & 1u) ? cc.add * inv_size[c] : 0.0;
+    double t = ((seeds[row] >> c) & 1u) ? cc.add * inv_size[c] : 0.0;
+    if (rhs) t += (double)rhs[(size_t)row * KT + c];
     y = (T)((double)beta * (double)acc + t);
     r_acc += fabs((double)y - (double)old);
   }
@@ -102,8 +105,8 @@ __global__ void __launch_bounds__(256) ppr_spmm_kernel(const int4 *__restrict__ 
                                                       const unsigned char *__restrict__ dmask,
                                                       const ColCtl *__restrict__ col,
                                                       const double *__restrict__ inv_size, double beta,
-                                                      T *__restrict__ chunk_partials, double *partials,
-                                                      const TileCtl *tile) {
+                                                      const T *__restrict__ rhs, T *__restrict__ chunk_partials,
+                                                      double *partials, const TileCtl *tile) {
   if (*(volatile const int *)&tile->done) return;
   const int c = threadIdx.x & (KT - 1);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
@@ -126,7 +129,7 @@ __global__ void __launch_bounds__(256) ppr_spmm_kernel(const int4 *__restrict__ 
     }
     for (; e < it.z; ++e) acc = fma(__ldg(values + e), __ldg(xo + (size_t)__ldg(colidx + e) * KT + c), acc);
     if (it.w >= 0) chunk_partials[(size_t)it.w * KT + c] = acc;
-    else ppr_emit<T, KT>(it.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, r_acc, d_acc);
+    else ppr_emit<T, KT>(it.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, rhs, r_acc, d_acc);
   }
   block_columns<KT>(r_acc, d_acc, partials, blockIdx.x);
 }
@@ -140,7 +143,8 @@ __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__
                                                        const unsigned char *__restrict__ dmask,
                                                        const ColCtl *__restrict__ col,
                                                        const double *__restrict__ inv_size, double beta,
-                                                       double *partials, int part_base, const TileCtl *tile) {
+                                                       const T *__restrict__ rhs, double *partials, int part_base,
+                                                       const TileCtl *tile) {
   if (*(volatile const int *)&tile->done) return;
   const int c = threadIdx.x & (KT - 1);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__
     const int2 h = crow[g];
     T acc = 0;
     for (int s = h.y; s < crow[g + 1].y; ++s) acc += chunk_partials[(size_t)s * KT + c];
-    ppr_emit<T, KT>(h.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, r_acc, d_acc);
+    ppr_emit<T, KT>(h.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, rhs, r_acc, d_acc);
   }
   block_columns<KT>(r_acc, d_acc, partials, part_base + blockIdx.x);
 }
@@ -157,7 +161,7 @@ __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__
 // per column: sum the parts in order, advance the column, then the tile
 template <int KT>
 __global__ void ppr_finalize_kernel(const double *__restrict__ partials, int nparts, ColCtl *col, TileCtl *tile,
-                                    double beta, double tol, int max_iter, int k_in_tile, int first) {
+                                    double beta, double cst, int max_iter, int k_in_tile, int first) {
   __shared__ int active;
   if (threadIdx.x == 0) active = 0;
   __syncthreads();
@@ -171,14 +175,14 @@ __global__ void ppr_finalize_kernel(const double *__restrict__ partials, int npa
     }
     ColCtl &cc = col[c];
     if (first) {
-      cc.add = beta * d + (1.0 - beta);  // initial vector: only the dangling mass is new
+      cc.add = beta * d + cst;  // initial vector: only the dangling mass is new
     } else if (!cc.done) {
       cc.iter += 1;
       cc.resid = r;
-      cc.add = beta * d + (1.0 - beta);
-      cc.done = r < tol || cc.iter >= max_iter;
+      cc.add = beta * d + cst;
+      cc.done = r < cc.tol || cc.iter >= max_iter;
     } else {
-      cc.add = beta * d + (1.0 - beta);
+      cc.add = beta * d + cst;
     }
     if (c < k_in_tile && !cc.done) atomicOr(&active, 1);
   }
@@ -204,6 +208,27 @@ __global__ void __launch_bounds__(256) ppr_init_kernel(int n, const unsigned *__
     if (dmask[i]) d_acc += (double)v;
   }
   block_columns<KT>(0.0, d_acc, partials, blockIdx.x);
+}
+
+// x (one tile) from FP64 vectors in the original labels: vector vec[c] of
+// src (src + vec[c] * n) at tile row newid[u] (u when not relabelled);
+// columns with vec[c] < 0 get 0.  With partials: the dangling mass per column.
+template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_load_kernel(int n, const double *__restrict__ src,
+                                                      const int *__restrict__ vec, const int *__restrict__ newid,
+                                                      const unsigned char *__restrict__ dmask, T *__restrict__ x,
+                                                      double *partials) {
+  const int c = threadIdx.x & (KT - 1);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
+  const int v = vec[c];
+  double d_acc = 0;
+  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; u < n; u += ng) {
+    const int i = newid ? newid[u] : (int)u;
+    const T val = v >= 0 ? (T)src[(size_t)v * n + u] : T(0);
+    x[(size_t)i * KT + c] = val;
+    if (partials && dmask[i]) d_acc += (double)val;
+  }
+  if (partials) block_columns<KT>(0.0, d_acc, partials, blockIdx.x);
 }
 
 // dmask[j] = 1 when column j holds no nonzero value
@@ -245,10 +270,22 @@ __global__ void ppr_move_kernel(const T *__restrict__ src, T *__restrict__ dst, 
   }
 }
 
+// Options of one batched solve: by default x0 = v_c and the teleport form
+// x = beta A x + (beta d.x + 1 - beta) v_c.  A defect-correction solve passes
+// x0 = rhs = r_c and cst = 0: e = beta A e + beta (d.e) v_c + r_c.
+struct RunOpts {
+  const double *x0 = nullptr;   // start: vector c at x0 + src(c) * n (original labels), FP64
+  const double *rhs = nullptr;  // added to every sweep: rhs + src(c) * n
+  const int *src = nullptr;     // host: column of x0 / rhs for vector c (NULL: c)
+  double cst = -1.0;            // the constant of the teleport term (< 0: 1 - beta)
+  const double *tol = nullptr;  // host: stopping threshold per vector (NULL: p->tol)
+};
+
 template <typename T, int KT>
 tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std::vector<int> *newid_host,
                          const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
-                         double *d_out, int *iters_out, double *resid_out, cudaStream_t s) {
+                         double *d_out, int *iters_out, double *resid_out, cudaStream_t s,
+                         const RunOpts &opt = RunOpts()) {
   const int n = M->n_row;
   const int64_t nnz = M->stored;
   const T *values = static_cast<const T *>(M->values[std::is_same<T, double>::value ? 0 : 1]);
@@ -306,6 +343,8 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   double *d_inv = nullptr, *partials = nullptr;
   ColCtl *d_col = nullptr;
   TileCtl *d_tile = nullptr;
+  T *rhs_t[2] = {nullptr, nullptr};  // the right-hand side in the tiles' layout (ping-pong for repacking)
+  int *d_vec = nullptr;              // per slot: the column of x0 / rhs it holds, or -1
   std::vector<void *> owned;
   tbsla_status_t st = TBSLA_OK;
   auto alloc = [&](void **ptr, size_t bytes) {
@@ -328,14 +367,24 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   alloc((void **)&partials, (size_t)tiles * nparts * KT * 2 * sizeof(double));
   alloc((void **)&d_col, (size_t)tiles * KT * sizeof(ColCtl));
   alloc((void **)&d_tile, (size_t)tiles * sizeof(TileCtl));
+  alloc((void **)&d_vec, (size_t)tiles * KT * sizeof(int));
+  if (opt.rhs) {
+    alloc((void **)&rhs_t[0], (size_t)tiles * xbytes);
+    alloc((void **)&rhs_t[1], (size_t)tiles * xbytes);
+  }
   auto cleanup = [&]() {
     cudaStreamSynchronize(s);
     for (void *q : owned) cudaFree(q);
   };
   if (st != TBSLA_OK) { cleanup(); return st; }
+  const double cst = opt.cst < 0 ? 1.0 - p->beta : opt.cst;
+  auto src_col = [&](int v) { return v < 0 ? -1 : opt.src ? opt.src[v] : v; };
   std::vector<ColCtl> hcol((size_t)tiles * KT);
+  std::vector<int> hvec((size_t)tiles * KT, -1);
   for (int c = 0; c < tiles * KT; ++c) {
-    hcol[(size_t)c] = ColCtl{0.0, 0.0, 0, c >= k ? 1 : 0};  // padding columns start stopped
+    // padding columns start stopped
+    hcol[(size_t)c] = ColCtl{0.0, 0.0, c < k && opt.tol ? opt.tol[c] : p->tol, 0, c >= k ? 1 : 0};
+    hvec[(size_t)c] = src_col(c < k ? c : -1);
   }
   std::vector<TileCtl> htile((size_t)tiles, TileCtl{0, 0, {0, 0}});
   if (p->max_iter == 0)
@@ -350,17 +399,26 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   up(d_inv, inv.data(), inv.size() * sizeof(double));
   up(d_col, hcol.data(), hcol.size() * sizeof(ColCtl));
   up(d_tile, htile.data(), htile.size() * sizeof(TileCtl));
+  up(d_vec, hvec.data(), hvec.size() * sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(dmask, 1, (size_t)n, s);
   if (e != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank upload: %s", cudaGetErrorString(e)); }
   ppr_dangling_kernel<T><<<152 * 8, 256, 0, s>>>(M->idx1, values, nnz, dmask);
   const double beta = p->beta;
   for (int t = 0; t < tiles; ++t) {
     double *pt = partials + (size_t)t * nparts * KT * 2;
-    ppr_init_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, d_seeds + (size_t)t * n, dmask, d_inv + (size_t)t * KT,
-                                                   x[0] + (size_t)t * n * KT, pt);
-    ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, grid_in, d_col + (size_t)t * KT, d_tile + t, beta, p->tol,
+    if (opt.x0)
+      ppr_load_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, opt.x0, d_vec + (size_t)t * KT, newid_dev, dmask,
+                                                     x[0] + (size_t)t * n * KT, pt);
+    else
+      ppr_init_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, d_seeds + (size_t)t * n, dmask, d_inv + (size_t)t * KT,
+                                                     x[0] + (size_t)t * n * KT, pt);
+    if (opt.rhs)
+      ppr_load_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, opt.rhs, d_vec + (size_t)t * KT, newid_dev, dmask,
+                                                     rhs_t[0] + (size_t)t * n * KT, nullptr);
+    ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, grid_in, d_col + (size_t)t * KT, d_tile + t, beta, cst,
                                              p->max_iter, std::min(KT, k - t * KT), 1);
   }
+  int rbase = 0;  // rhs_t[rbase] holds the current layout's right-hand side
   if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank init"); }
   // Sweeps in rounds of K on every tile of the current layout (stopped tiles
   // return at once).  After each round the vectors that stopped are written
@@ -389,13 +447,14 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
         const unsigned *sd = d_seeds + (size_t)t * n;
         const ColCtl *cl = d_col + (size_t)t * KT;
         const double *iv = d_inv + (size_t)t * KT;
+        const T *rh = opt.rhs ? rhs_t[rbase] + (size_t)t * n * KT : nullptr;
         ppr_spmm_kernel<T, KT><<<grid_mm, 256, 0, s>>>(d_items, (int)items.size(), M->idx1, values, xo, xn, sd,
-                                                       dmask, cl, iv, beta, chunk, pt, d_tile + t);
+                                                       dmask, cl, iv, beta, rh, chunk, pt, d_tile + t);
         if (n_crow)
           ppr_fixup_kernel<T, KT><<<grid_fx, 256, 0, s>>>(d_crow, n_crow, chunk, xo, xn, sd, dmask, cl, iv, beta,
-                                                          pt, grid_mm, d_tile + t);
+                                                          rh, pt, grid_mm, d_tile + t);
         ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm, d_col + (size_t)t * KT,
-                                                 d_tile + t, beta, p->tol, p->max_iter, KT, 0);
+                                                 d_tile + t, beta, cst, p->max_iter, KT, 0);
       }
     }
     if (cudaMemcpyAsync(htc.data(), d_tile, (size_t)cur_tiles * sizeof(TileCtl), cudaMemcpyDeviceToHost, s) !=
@@ -457,7 +516,7 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
           for (int u : seed_sets[(size_t)v]) nseeds[(size_t)(q / KT) * n + u] |= 1u << (q % KT);
           ++q;
         }
-      for (size_t r = (size_t)q; r < ncol.size(); ++r) ncol[r] = ColCtl{0.0, 0.0, 0, 1};
+      for (size_t r = (size_t)q; r < ncol.size(); ++r) ncol[r] = ColCtl{0.0, 0.0, 0.0, 0, 1};
       std::vector<TileCtl> ntile((size_t)need, TileCtl{0, 0, {0, 0}});
       up(d_map, map.data(), map.size() * sizeof(int));
       up(d_seeds, nseeds.data(), nseeds.size() * sizeof(unsigned));
@@ -467,6 +526,10 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
       if (e != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack: %s", cudaGetErrorString(e)); }
       const int src = (base + phase) & 1;
       ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(x[src], x[src ^ 1], n, d_map, need);
+      if (opt.rhs) {
+        ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(rhs_t[rbase], rhs_t[rbase ^ 1], n, d_map, need);
+        rbase ^= 1;
+      }
       if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack"); }
       base = src ^ 1;
       phase = 0;
@@ -481,6 +544,91 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     return fail(TBSLA_ERR_CUDA, "batched PageRank results");
   }
   cleanup();
+  return TBSLA_OK;
+}
+
+__global__ void ppr_sub_kernel(double *__restrict__ g, const double *__restrict__ x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    g[i] -= x[i];
+}
+__global__ void ppr_add_kernel(double *__restrict__ x, const double *__restrict__ e, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += e[i];
+}
+
+// FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined):
+// x = the FP32 solve; then rounds of r = G(x) - x by one FP64 sweep of every
+// vector, stopping when every ||r_c||_1 < tol (the result is G(x)), else the
+// FP32 correction solve e = beta A e + beta (d.e) v_c + r_c from e = r_c to
+// ||e_j+1 - e_j||_1 < eta ||r_c||_1, and x += e.  Iterations: FP32 and FP64
+// sweeps together.
+constexpr double kRefineEta = 1e-3;     // inner tolerance relative to ||r_c||_1
+constexpr double kF32SolveFloor = 1e-6; // the FP32 solve's stopping threshold at least this
+constexpr int kRefineRounds = 8;
+
+template <int KT>
+tbsla_status_t run_refined(const tbsla_matrix *M, const int *nd, const std::vector<int> *nh,
+                           const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
+                           double *d_out, int *iters_out, double *resid_out, cudaStream_t s) {
+  const int64_t n = M->n_row, total = n * k;
+  std::vector<int> itot((size_t)k), it((size_t)k);
+  std::vector<double> res((size_t)k, 0.0), tolc((size_t)k);
+  tbsla_pagerank_params_t q = *p;
+  q.tol = std::max(p->tol, kF32SolveFloor);
+  TB_TRY((run_tiles<float, KT>(M, nd, nh, &q, k, nodes, offsets, d_out, itot.data(), nullptr, s)));
+  double *g = nullptr, *e = nullptr;
+  TB_CUDA(cudaMallocAsync((void **)&g, (size_t)total * sizeof(double), s));
+  if (cudaMallocAsync((void **)&e, (size_t)total * sizeof(double), s) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFreeAsync(g, s);
+    return fail(TBSLA_ERR_OOM, "refinement buffers (2 x %lld doubles)", (long long)total);
+  }
+  struct Free {
+    cudaStream_t s;
+    double *a, *b;
+    ~Free() {
+      cudaFreeAsync(a, s);
+      cudaFreeAsync(b, s);
+      cudaStreamSynchronize(s);
+    }
+  } release{s, g, e};
+  const int grid = 152 * 8;
+  for (int round = 0;; ++round) {
+    // r = G(x) - x: one FP64 sweep from x (the sweep's L1 change is ||r_c||_1)
+    tbsla_pagerank_params_t q64 = *p;
+    q64.max_iter = 1;
+    RunOpts o64;
+    o64.x0 = d_out;
+    TB_TRY((run_tiles<double, KT>(M, nd, nh, &q64, k, nodes, offsets, g, nullptr, res.data(), s, o64)));
+    bool all = true;
+    for (int c = 0; c < k; ++c) {
+      itot[(size_t)c] += 1;
+      all = all && res[(size_t)c] < p->tol;
+    }
+    if (all || round == kRefineRounds) {
+      TB_CUDA(cudaMemcpyAsync(d_out, g, (size_t)total * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      break;
+    }
+    ppr_sub_kernel<<<grid, 256, 0, s>>>(g, d_out, total);
+    TB_CUDA(cudaGetLastError());
+    // the correction, only as far as each vector still needs it
+    for (int c = 0; c < k; ++c)
+      tolc[(size_t)c] = res[(size_t)c] < p->tol ? HUGE_VAL : kRefineEta * res[(size_t)c];
+    RunOpts oc;
+    oc.x0 = g;
+    oc.rhs = g;
+    oc.cst = 0.0;
+    oc.tol = tolc.data();
+    TB_TRY((run_tiles<float, KT>(M, nd, nh, p, k, nodes, offsets, e, it.data(), nullptr, s, oc)));
+    for (int c = 0; c < k; ++c) itot[(size_t)c] += it[(size_t)c];
+    ppr_add_kernel<<<grid, 256, 0, s>>>(d_out, e, total);
+    TB_CUDA(cudaGetLastError());
+  }
+  TB_CUDA(cudaStreamSynchronize(s));
+  for (int c = 0; c < k; ++c) {
+    if (iters_out) iters_out[c] = itot[(size_t)c];
+    if (resid_out) resid_out[c] = res[(size_t)c];
+  }
   return TBSLA_OK;
 }
 
@@ -502,9 +650,9 @@ tbsla_status_t run_kt(int kt, const tbsla_matrix *M, const int *nd, const std::v
 
 using namespace tbsla;
 
-extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
-                                            const int *nodes, const int *offsets, int tile, double *d_out,
-                                            int *iterations, double *residuals, void *stream) {
+static tbsla_status_t ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                  const int *nodes, const int *offsets, int tile, double *d_out, int *iterations,
+                                  double *residuals, void *stream, bool refined) {
   TB_CHECK(A && p && nodes && offsets && d_out, "NULL argument");
   TB_CHECK(k > 0, "k = %d", k);
   TB_CHECK(A->format == TBSLA_FMT_CSR, "batched PageRank needs a CSR handle");
@@ -525,6 +673,30 @@ extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla
   // 10.5 / 9.7 / 9.3 / 8.5 for tiles 2 / 4 / 8 / 16 / 32)
   const int kt = tile ? tile : tuned ? tuned : (k >= 32 ? 32 : k >= 16 ? 16 : k >= 8 ? 8 : k >= 4 ? 4 : 2);
   cudaStream_t s = (cudaStream_t)stream;
+  if (refined) {
+    TB_CHECK(p->precision == TBSLA_F32, "the refined batched solve takes TBSLA_F32");
+    TB_CHECK(R->values[0] && R->values[1], "the refined batched solve needs the F64 and F32 value stores");
+    switch (kt) {
+    case 2: return run_refined<2>(R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+    case 4: return run_refined<4>(R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+    case 8: return run_refined<8>(R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+    case 16: return run_refined<16>(R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+    default: return run_refined<32>(R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+    }
+  }
   if (p->precision == TBSLA_F64) return run_kt<double>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
   return run_kt<float>(kt, R, nd, nh, p, k, nodes, offsets, d_out, iterations, residuals, s);
+}
+
+extern "C" tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
+                                            const int *nodes, const int *offsets, int tile, double *d_out,
+                                            int *iterations, double *residuals, void *stream) {
+  return ppr_batched(A, p, k, nodes, offsets, tile, d_out, iterations, residuals, stream, false);
+}
+
+extern "C" tbsla_status_t tbsla_ppr_batched_refined(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p,
+                                                    int k, const int *nodes, const int *offsets, int tile,
+                                                    double *d_out, int *iterations, double *residuals,
+                                                    void *stream) {
+  return ppr_batched(A, p, k, nodes, offsets, tile, d_out, iterations, residuals, stream, true);
 }

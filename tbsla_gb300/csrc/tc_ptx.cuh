@@ -71,6 +71,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
   }
 }
 
+// ------------------------------------------- programmatic dependent launch
+// Waits until the grids this launch depends on (the stream's previous
+// kernels) have completed and their memory is visible; a no-op for a launch
+// without the programmatic-serialization attribute.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the stream's next kernel, when launched with programmatic
+// serialization, start before this grid completes.
+__device__ __forceinline__ void grid_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ------------------------------------------------------------------ TMA
 // L2 policies for the streamed operand (evict first) and the reused one
 __device__ __forceinline__ uint64_t policy_evict_first() {

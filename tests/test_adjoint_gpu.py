@@ -211,3 +211,25 @@ def test_autograd_shim_gradcheck(gpu, orc):
     assert torch.autograd.gradcheck(f, (pv, tv), eps=1e-7, atol=1e-7, rtol=1e-5)
     f0 = lambda a, b: (ag.pagerank(P, a, b, tol=1e-15, accel=0) * wt).sum()
     assert torch.autograd.gradcheck(f0, (pv, tv), eps=1e-7, atol=1e-7, rtol=1e-5)
+
+
+def test_adjoint_against_finite_differences_rmat_2p22(gpu):
+    """The differentiation configuration's graph (R-MAT 2^22, 2^26 draws,
+    seed 1; w ~ N(0,1) seed 2): the adjoint values gradient against central
+    fourth-order differences of the GPU forward solve on 60 random edges
+    (bench.py checks 1000), relative error <= 1e-6."""
+    import bench
+    scale = 22
+    G = gpu.DeviceMatrix.rmat_pagerank(scale, 16 << scale, seed=1)
+    n, nnz = G.info().n_row, int(G.info().stored)
+    dev = torch.device("cuda")
+    w = torch.from_numpy(np.random.default_rng(2).standard_normal(n)).to(dev)
+    v = torch.full((n,), 1.0 / n, dtype=torch.float64, device=dev)
+    x = torch.empty(n, dtype=torch.float64, device=dev)
+    gvals = torch.empty(nnz, dtype=torch.float64, device=dev)
+    G.pagerank_teleport(v.data_ptr(), x.data_ptr(), 0.85, 1e-15, 2000, accel=1)
+    r = G.pagerank_adjoint(v.data_ptr(), x.data_ptr(), w.data_ptr(), gvals.data_ptr(), 0, 0.85, n * 1e-15, 2000,
+                           accel=1)
+    assert r.converged
+    fd = bench.fd_check_edges(gpu, G, v, w, gvals.cpu().numpy(), 60, seed=11)
+    assert fd["rel_err_max"] <= 1e-6, fd

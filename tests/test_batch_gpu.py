@@ -102,6 +102,18 @@ def test_batched_ppr_matches_oracle(gpu, orc, tile, relabel):
                                    precision=gpu.F32)
     got32 = out32.cpu().numpy().reshape(k, n)
     assert np.max(np.abs(got32 - got).sum(axis=1)) < 1e-5
+    # FP32 sweeps with FP64 defect correction: every vector to the FP64 tolerance
+    outr = torch.empty(k * n, dtype=torch.float64, device=dev)
+    itsr, resr = gpu.ppr_batched(A, sets, outr.data_ptr(), tol=1e-12, max_iter=1000, tile=tile,
+                                 precision=gpu.F32, refined=True)
+    assert (resr < 1e-12).all(), resr.max()
+    gotr = outr.cpu().numpy().reshape(k, n)
+    for c in (0, 1, 7, 20, 39):
+        v = np.zeros(n)
+        seeds = np.unique(sets[c])
+        v[seeds] = 1.0 / seeds.size
+        xo, _, _ = orc.pagerank_teleport(rp, ci, va, dang, v, 0.85, 1e-14, 2000)
+        assert np.abs(gotr[c] - xo).sum() < 1e-11, (c, np.abs(gotr[c] - xo).sum())
 
 
 @pytest.mark.parametrize("tile,check_every,prec", [(8, 1, "F64"), (4, 3, "F64"), (32, 2, "F32")])

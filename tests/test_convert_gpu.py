@@ -119,3 +119,53 @@ def test_csr_normalize_columns(gpu, orc):
         B = gpu.DeviceMatrix.csr(nr, nc, rp, ci, ov)
         xc = rng.uniform(-1, 1, nc)
         assert np.array_equal(m.spmv_host(xc), B.spmv_host(xc))
+
+
+def _device_vs_oracle(gpu, orc, fmt, gen, nr, nc, c, q, s, blk):
+    """A handle from tbsla_generate_device against the oracle's fill of the
+    same block: the arrays bit for bit, and the same info as the handle the
+    host arrays give."""
+    A = gpu.DeviceMatrix.generate_device(fmt, gen, nr, nc, c, q, s, *blk)
+    fill = {"cdiag": lambda: orc.fill_cdiag(fmt, nr, nc, c, *blk),
+            "cqmat_stochastic": lambda: orc.fill_cqmat_stochastic(fmt, nr, nc, c, q, s, *blk)}[gen]
+    a = fill().arrays
+    H = gpu.DeviceMatrix.from_generated(gpu.generate(fmt, gen, nr, nc, c, q, s, *blk))
+    i, h = A.info(), H.info()
+    tag = (fmt, gen, nr, nc, c, q, s, blk)
+    assert (i.n_row, i.n_col, i.f_col, i.rows, i.max_col, i.stored) == \
+        (h.n_row, h.n_col, h.f_col, h.rows, h.max_col, h.stored), tag
+    if fmt == "CSR":
+        rp, ci, va = A.csr_download()
+        if a.values.size:
+            assert np.array_equal(rp, a.idx0) and np.array_equal(ci, a.idx1), tag
+        assert np.array_equal(va, a.values), tag
+    elif fmt == "ELL":
+        cols, vals = A.ell_download()
+        assert np.array_equal(cols, a.idx0[: cols.size]) and np.array_equal(vals, a.values[: vals.size]), tag
+    else:
+        assert np.array_equal(A.dense_download(), a.values), tag
+    x = np.random.default_rng(1).uniform(-1, 1, nc)
+    assert np.array_equal(A.spmv_host(x), H.spmv_host(x)), tag
+
+
+@pytest.mark.parametrize("fmt", ["CSR", "ELL", "DENSE"])
+def test_device_generators_match_oracle(gpu, orc, fmt):
+    """fill_cdiag generated on the device and fill_cqmat_stochastic divided on
+    the device (tbsla_generate_device) give the reference's arrays for whole
+    matrices and blocks, square and not."""
+    blocks = [(0, 0, 1, 1), (1, 0, 2, 1), (0, 1, 1, 2), (1, 2, 3, 4)]
+    for (nr, nc) in [(30, 30), (50, 20), (20, 50), (1, 1)]:
+        for blk in blocks:
+            for c in (0, 1, 3, 25):
+                _device_vs_oracle(gpu, orc, fmt, "cdiag", nr, nc, c, 0.0, 0, blk)
+            for (c, q, s) in [(5, 0.1, 1), (8, 0.5, 3)]:
+                _device_vs_oracle(gpu, orc, fmt, "cqmat_stochastic", nr, nc, c, q, s, blk)
+    if fmt == "CSR":
+        # the format sweep's cdiag case at 2^26 rows and a 2^20 stochastic matrix
+        n = 1 << 26
+        A = gpu.DeviceMatrix.generate_device("CSR", "cdiag", n, n, 1)
+        rp, ci, va = A.csr_download()
+        assert rp[-1] == 2 * n - 2 and np.all(va == 1.0)
+        assert np.array_equal(rp[:4], [0, 1, 3, 5]) and np.array_equal(ci[:5], [1, 0, 2, 1, 3])
+        assert ci[-1] == n - 2
+        _device_vs_oracle(gpu, orc, "CSR", "cqmat_stochastic", 1 << 20, 1 << 20, 16, 0.1, 0, (0, 0, 1, 1))

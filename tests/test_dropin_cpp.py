@@ -68,8 +68,51 @@ def _registered_reference_tests() -> list[str]:
         return []
     exe = dict(re.findall(r"add_executable\((\w+)\s+(\w+\.cpp)\)", open(cm).read()))
     tested = re.findall(r"add_test\(\w+\s+(\w+)\)", open(cm).read())
-    # input_parser tests the command-line parser of the reference's apps
-    return sorted({exe[t] for t in tested if t in exe and exe[t] != "input_parser.cpp"})
+    return sorted({exe[t] for t in tested if t in exe})
+
+
+REFERENCE_APPS = os.path.join(_REF_SRC, "apps") if _REF_SRC else ""
+
+
+def _reference_apps() -> list[str]:
+    if not os.path.isdir(REFERENCE_APPS):
+        return []
+    return sorted(f for f in os.listdir(REFERENCE_APPS) if f.endswith(".cpp"))
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_APPS), reason="TBSLA sources not present")
+@pytest.mark.parametrize("src", _reference_apps() or ["none"])
+def test_reference_apps_compile_against_dropin(capi, tmp_path, src):
+    """The reference's driver programs (src/cpp/apps/*.cpp: tbsla_perf,
+    tbsla_page_rank, ...) build unchanged against the drop-in headers
+    (InputParser.hpp, split.hpp, cpuset_to_cstr.hpp, tbsla/Configs.h among
+    them) and the library."""
+    lib_dir = os.path.dirname(capi.LIB_PATH)
+    r = _compile_cpp(os.path.join(REFERENCE_APPS, src), str(tmp_path / "t"), lib_dir)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_TESTS), reason="TBSLA sources not present")
+def test_reference_input_parser_test_passes(capi, tmp_path):
+    """The reference's command-line parser test (src/cpp/tests/input_parser.cpp)
+    runs against the drop-in's InputParser (no GPU involved) and exits 0."""
+    lib_dir = os.path.dirname(capi.LIB_PATH)
+    exe = str(tmp_path / "input_parser")
+    r = _compile_cpp(os.path.join(REFERENCE_TESTS, "input_parser.cpp"), exe, lib_dir)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert subprocess.run([exe], timeout=60).returncode == 0
+
+
+def test_driver_utilities(capi, tmp_path):
+    """split, cpuset_to_cstr and InputParser of the drop-in on known answers
+    (the behaviour of src/cpp/utils/split.cpp, cpuset_to_cstr.cpp and
+    InputParser.cpp)."""
+    lib_dir = os.path.dirname(capi.LIB_PATH)
+    exe = str(tmp_path / "utils_check")
+    r = _compile_cpp(os.path.join(ROOT, "tests", "cpp", "utils_check.cpp"), exe, lib_dir)
+    assert r.returncode == 0, r.stderr[-2000:]
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, run.stdout + run.stderr
 
 
 @pytest.mark.skipif(not os.path.isdir(REFERENCE_TESTS), reason="TBSLA sources not present")
