@@ -427,7 +427,8 @@ def pagerank_bench(capi, scale=24, cpu=True):
            "reference_solve": {"tol": 1e-13, "sweeps": r.iterations, "converged": bool(r.converged)}}
     times, gpu_vectors = {}, {}
     for name, prec, acc in (("fp64", capi.F64, 0), ("fp32_refined", capi.F32, 0), ("bf16_refined", capi.BF16, 0),
-                            ("fp64_anderson", capi.F64, 1)):
+                            ("fp64_anderson", capi.F64, 1), ("fp32_refined_anderson", capi.F32, 1),
+                            ("bf16_refined_anderson", capi.BF16, 1)):
         A.pagerank(out.data_ptr(), tol=1e-10, max_iter=2000, precision=prec, accel=acc)  # warm: workspace + graphs
         torch.cuda.synchronize()
         ts = []
@@ -444,6 +445,12 @@ def pagerank_bench(capi, scale=24, cpu=True):
     res["bf16_over_fp64_time"] = round(times["bf16_refined"] / times["fp64"], 3)
     res["anderson_over_fp64_time"] = round(times["fp64_anderson"] / times["fp64"], 3)
     res["fp32_over_fp64_time"] = round(times["fp32_refined"] / times["fp64"], 3)
+    # the precision form with accelerated correction solves, against the plain
+    # FP64 solve (the ratio the target names) and the accelerated FP64 one
+    res["fp32_anderson_refined_over_fp64_time"] = round(times["fp32_refined_anderson"] / times["fp64"], 3)
+    res["bf16_anderson_refined_over_fp64_time"] = round(times["bf16_refined_anderson"] / times["fp64"], 3)
+    res["fp32_anderson_refined_over_fp64_anderson_time"] = round(times["fp32_refined_anderson"] /
+                                                                  times["fp64_anderson"], 3)
     # Matrix::page_rank (reference mode: max-normalised, no dangling term) at
     # the reference's epsilon 1e-9 on the same graph
     A.pagerank(out.data_ptr(), beta=0.85, tol=1e-9, max_iter=1000, mode=capi.PR_REFERENCE)

@@ -109,6 +109,12 @@ def test_dangling_mode_fp64_and_mixed(gpu, orc, scale):
     assert r.converged and r.residual < 1e-11
     assert abs(x.sum() - 1.0) < 1e-12
     assert np.abs(x - xo).sum() < 1e-10, (r.iterations, np.abs(x - xo).sum())
+    # mixed precision with Anderson-accelerated inner (correction) solves
+    for prec in (gpu.F32, gpu.BF16):
+        xm, rm = A.pagerank_host(beta=0.85, tol=1e-11, max_iter=5000, mode=gpu.PR_DANGLING, precision=prec,
+                                 accel=1)
+        assert rm.converged and abs(xm.sum() - 1.0) < 1e-12, prec
+        assert np.abs(xm - xo).sum() < 1e-10, (prec, np.abs(xm - xo).sum(), rm.iterations, rm.iterations_f64)
     # (at scale 10 the plain iteration converges as fast: 17 sweeps both)
     assert r.iterations <= sweeps[gpu.F64] - (2 if scale >= 14 else 0), (r.iterations, sweeps[gpu.F64])
 
