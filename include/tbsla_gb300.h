@@ -383,13 +383,17 @@ typedef struct {
                          vectors, corrected by FP64 residual refinement
                          (TBSLA_PR_DANGLING only; needs TBSLA_STORE_F64 too) */
   int check_every;    /* sweeps per convergence check (0: library default) */
-  int accel;          /* FP64 dangling and teleport modes, and the adjoint:
+  int accel;          /* dangling and teleport modes, and the adjoint:
                          0 power iteration; 1 Anderson acceleration over
                          the last two differences (the next sweep starts
                          from the combination of the last three sweep
                          outputs whose residual combination is smallest in
                          the 2-norm); same stopping rule, same fixed point,
-                         fewer sweeps */
+                         fewer sweeps.  With precision TBSLA_F32 / TBSLA_BF16
+                         the low-precision correction solves are the
+                         accelerated ones (FP32 vectors; an F32 store is
+                         then solved to 1e-4 of ||r|| per correction, BF16
+                         to 0.05) */
 } tbsla_pagerank_params_t;
 
 typedef struct {
