@@ -646,10 +646,18 @@ def fd_check_edges(capi, G, v, w, gvals, n_edges, seed=7, sweeps=30):
     (teleport form, Anderson-accelerated, a fixed `sweeps` sweeps with no
     stopping test, which reaches FP64 rounding: the same count for every
     perturbation keeps L a smooth function of the step), against the adjoint's
-    gradient gvals.  Perturbing one entry is a rank-one change of the fixed
-    point's system, so L(t) = L0 + g t / (1 - c t) exactly and the
-    differences (8(L(h) - L(-h)) - (L(2h) - L(-2h))) / 12h equal g (1 - 4 c^4
-    h^4); h = 3e-3 of the entry.  Returns the relative errors' summary."""
+    gradient gvals.
+
+    Perturbing one entry is a rank-one change of the fixed point's system, so
+    L(t) = L0 + g t / (1 - c t) exactly, and the differences
+    (8(L(h) - L(-h)) - (L(2h) - L(-2h))) / 12h equal g (1 - 4 c^4 h^4).  L
+    carries about one unit in the last place of rounding (~2e-18 here), so a
+    step of 3e-3 of the entry drowns the smallest gradients (2e-9: 4e-5
+    relative); the step is that, raised where needed to make |g| h reach
+    2e-10, at most a quarter of the entry.  Also reported: the rank-one
+    estimate g = 2 / (h (1/(L(h) - L0) - 1/(L(-h) - L0))), exact for any
+    step, from the same solves and one unperturbed solve.  Returns the
+    relative errors' summary."""
     import torch
     dev = torch.device("cuda")
     _, _, vals = G.csr_download()
@@ -664,22 +672,30 @@ def fd_check_edges(capi, G, v, w, gvals, n_edges, seed=7, sweeps=30):
         return float(torch.dot(w, xx).item())
 
     t0 = time.perf_counter()
-    rel = []
+    l0 = loss()
+    rel, rel_rank1, steps = [], [], []
     for e in edges:
         e = int(e)
-        h = 3e-3 * vals[e]
+        a = vals[e]
+        h = max(3e-3 * a, min(0.25 * a, 2e-10 / max(abs(gvals[e]), 1e-300)))
+        steps.append(h / a)
         f = []
         for s_ in (1, -1, 2, -2):
-            base[e] = vals[e] + s_ * h
+            base[e] = a + s_ * h
             f.append(loss())
-        base[e] = vals[e]
+        base[e] = a
         fd = (8 * (f[0] - f[1]) - (f[2] - f[3])) / (12 * h)
         rel.append(abs(gvals[e] - fd) / max(abs(fd), 1e-300))
+        r1 = 2.0 / (h * (1.0 / (f[0] - l0) - 1.0 / (f[1] - l0)))
+        rel_rank1.append(abs(gvals[e] - r1) / max(abs(r1), 1e-300))
     G.set_values(capi.F64, base.data_ptr())
-    rel = np.array(rel)
-    return {"edges": int(n_edges), "step": "3e-3 of the entry, fourth order", "forward_sweeps": sweeps,
+    rel, rel_rank1 = np.array(rel), np.array(rel_rank1)
+    return {"edges": int(n_edges), "order": 4, "forward_sweeps": sweeps,
+            "step_over_entry_min_median_max": [float(np.min(steps)), float(np.median(steps)), float(np.max(steps))],
             "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
-            "edges_above_1e-6": int((rel > 1e-6).sum()), "s": round(time.perf_counter() - t0, 1)}
+            "edges_above_1e-6": int((rel > 1e-6).sum()),
+            "rank_one_estimate_rel_err_max": float(rel_rank1.max()),
+            "s": round(time.perf_counter() - t0, 1)}
 
 
 def differentiation_bench(capi, scale=22):

@@ -30,7 +30,7 @@ def _write_mm(path, n, rows, cols, vals):
         fh.write("%%MatrixMarket matrix coordinate real general\n")
         fh.write(f"{n} {n} {len(vals)}\n")
         for r, c, v in zip(rows, cols, vals):
-            fh.write(f"{r + 1} {c + 1} {v!r}\n")
+            fh.write(f"{int(r) + 1} {int(c) + 1} {float(v)!r}\n")
 
 
 @pytest.mark.parametrize("fmt", ["COO", "CSR", "ELL"])
