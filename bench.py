@@ -293,6 +293,12 @@ def format_sweep(capi, peak, log2n=24):
         gbs = algo / (ms * 1e-3) / 1e9
         out[key] = {"ms": round(ms, 4), "GB_s": round(gbs, 1), "frac_hbm": round(gbs / peak, 3),
                     "stored": int(i.stored), "gflops": round(2 * i.stored / (ms * 1e-3) / 1e9, 1)}
+        if fmt in ("COO", "SCOO"):
+            # the direct kernels read a derived row pointer, not the row array:
+            # the bytes they move are the CSR product's
+            read = csr_bytes(i.n_row, i.n_col, i.stored, vb, xb)
+            out[key]["GB_s_of_bytes_read"] = round(read / (ms * 1e-3) / 1e9, 1)
+            out[key]["frac_hbm_of_bytes_read"] = round(read / (ms * 1e-3) / 1e9 / peak, 3)
         if gen == "cqmat" and fmt in ("CSR", "ELL", "COO", "SCOO") and store == capi.F64:
             # a_axpx_ (Matrix.cpp:6-11): two products and the "+ x" (fused
             # into the first product's epilogue); bytes 2 x the matrix + 5 n-vectors
@@ -576,6 +582,19 @@ def batching_bench(capi, ppr_scale=22):
         if prec == capi.F32:
             entry["max_l1_vs_fp64"] = float((buf.view(k, n) - ref.view(k, n)).abs().sum(dim=1).max().item())
         res[name] = entry
+    # FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined) to
+    # the FP64 tolerance; distance to the FP64 batched solve (itself at 1e-10)
+    buf = torch.empty(k * n, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    its, rs = capi.ppr_batched(G, sets, buf.data_ptr(), tol=1e-10, max_iter=1000, precision=capi.F32, refined=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    res["fp32_refined"] = {"s": round(dt, 3), "ms_per_vector": round(dt * 1e3 / k, 3),
+                           "sweeps_min_median_max": [int(its.min()), int(np.median(its)), int(its.max())],
+                           "converged": int((rs < 1e-10).sum()),
+                           "max_l1_vs_fp64": float((buf.view(k, n) - ref.view(k, n)).abs().sum(dim=1).max().item())}
+    del buf
     # one vector at a time (teleport form, same stopping rule)
     v = torch.zeros(n, dtype=torch.float64, device=dev)
     seeds = np.unique(sets[0])
