@@ -275,7 +275,10 @@ def format_sweep(capi, peak, log2n=24):
     for (key, fmt, gen, nn, c, stores, store, vt) in cases:
         # a cleared set-aside: no persisting lines of the previous case's x
         capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
-        A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE if gen == "cqmat" else 0.0, 0, stores=stores)
+        if gen == "cdiag":  # built on the device (tbsla_generate_device), the host fill's arrays
+            A = capi.DeviceMatrix.generate_device(fmt, gen, nn, nn, c, 0.0, 0, stores=stores)
+        else:
+            A = capi.DeviceMatrix.generate(fmt, gen, nn, nn, c, Q_HEADLINE, 0, stores=stores)
         A.tune(capi.TUNE_X_L2_KEEP, X_KEEP_HEADLINE if vt == capi.F64 else X_KEEP_FP32)
         A.tune(capi.TUNE_X_L2_RANGE, X_RANGE_HEADLINE)
         i = A.info()

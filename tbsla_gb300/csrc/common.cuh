@@ -95,6 +95,10 @@ struct tbsla_matrix {
   // items (long rows and chunks of huge rows), huge rows, chunk partials
   int *short_rows = nullptr;
   int n_short = 0;
+  // the first n_tiny entries of short_rows hold every short row of at most
+  // kTinyRow entries (empty ones included), when there are many of them:
+  // reducing epilogues (PageRank sweeps) run them in warp tiles
+  int n_tiny = 0;
   int64_t short_nnz = 0;  // entries of the short rows
   int short_max = 0;      // entries of the longest short row (<= kTinyRow, all rows
                           // short and in order: the tiny-row warp tiles)

@@ -286,6 +286,78 @@ __global__ void __launch_bounds__(256) csr_tiny_kernel(int n_rows, const int *__
   epi.block_done(es, blockIdx.x);
 }
 
+// Tiny rows from a list: rows[0..n) each hold at most T entries (empty ones
+// included), in any order.  As csr_tiny_kernel, a warp takes 32 R list
+// entries, lane l entries l, l + 32, ..., with the bounds, entries and
+// gathers of its R rows in flight together, but grid-stride over tiles, so
+// that a reducing epilogue's capped grid covers the list; one thread per row
+// would wait on each row's load chain in turn (PageRank sweeps on R-MAT:
+// four fifths of the rows).  Each row is summed in stored order, one FMA per
+// entry: the one-thread-per-row arithmetic.
+constexpr int kTinyListRows = 2;  // R: rows per lane
+inline int tiny_list_grid(int n, bool reduces) {
+  const int g = (int)(((int64_t)n + 256 * kTinyListRows - 1) / (256 * kTinyListRows));
+  return std::max(1, reduces ? std::min(g, 152 * 16) : g);
+}
+
+template <typename V, typename XT, typename Epi>
+__global__ void __launch_bounds__(256) csr_tiny_list_kernel(const int *__restrict__ rows, int n,
+                                                           const int *__restrict__ rowptr,
+                                                           const int *__restrict__ colidx,
+                                                           const V *__restrict__ values,
+                                                           const XT *__restrict__ x, int f_col, XKeep x_keep,
+                                                           Epi epi) {
+  using Acc = typename Epi::Acc;
+  constexpr int R = kTinyListRows, T = kTinyRow;
+  if (!epi.active()) return;
+  typename Epi::State es{};
+  const uint64_t keep = policy_keep(x_keep, x);
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 * R); base < n;
+       base += nwarps * (32 * R)) {
+    int r[R], a[R], b[R];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int64_t idx = base + lane + 32 * q;
+      r[q] = idx < n ? __ldg(rows + idx) : -1;
+    }
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      a[q] = r[q] >= 0 ? __ldg(rowptr + r[q]) : 0;
+      b[q] = r[q] >= 0 ? __ldg(rowptr + r[q] + 1) : 0;
+    }
+    V v[R][T];
+    int c[R][T];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      #pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const int k = a[q] + t;
+        const bool in = k < b[q];
+        c[q][t] = in ? ld_ell<false>(colidx + k) : f_col;
+        v[q][t] = in ? ld_ell<false>(values + k) : V(0);
+      }
+    }
+    Acc xv[R][T];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      #pragma unroll
+      for (int t = 0; t < T; ++t)
+        xv[q][t] = a[q] + t < b[q] ? to_acc(ld_keep(x + (c[q][t] - f_col), keep), Acc()) : Acc(0);
+    }
+    #pragma unroll
+    for (int q = 0; q < R; ++q) {
+      Acc acc = 0;
+      #pragma unroll
+      for (int t = 0; t < T; ++t)
+        if (a[q] + t < b[q]) acc = fma_acc(to_acc(v[q][t], Acc()), xv[q][t], acc);
+      if (r[q] >= 0) epi.emit(r[q], acc, es);
+    }
+  }
+  epi.block_done(es, blockIdx.x);
+}
+
 // sum of entries [a, b) by a group of L lanes of one warp (L a power of two
 // <= 32, groups aligned in the warp): lanes stride the range, fixed shuffle
 // tree within the group.  Valid in the group's first lane.

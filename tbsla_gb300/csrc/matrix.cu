@@ -461,6 +461,18 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
       for (int r = 0; r < rows; r += 32) cap = std::max(cap, rp[std::min(r + 32, rows)] - rp[r]);
       A->stage_cap = std::max(16, (cap + 15) / 16 * 16);
     }
+    // Rows of at most kTinyRow entries first, when they are a large part of
+    // the short rows (power-law graphs: R-MAT 2^22 has 52 % empty rows and
+    // 27 % of 1-4 entries); the order within each part is the rows' order.
+    A->n_tiny = 0;
+    if (!all_short && !shorts.empty()) {
+      int64_t tiny = 0;
+      for (int r : shorts) tiny += rp[r + 1] - rp[r] <= kTinyRow;
+      if (tiny >= 1024 && 8 * tiny >= (int64_t)shorts.size()) {
+        std::stable_partition(shorts.begin(), shorts.end(), [&](int r) { return rp[r + 1] - rp[r] <= kTinyRow; });
+        A->n_tiny = (int)tiny;
+      }
+    }
     if (!all_short && !shorts.empty()) {
       TB_TRY(alloc_n(A, &A->short_rows, (int64_t)shorts.size()));
       TB_CUDA(cudaMemcpy(A->short_rows, shorts.data(), shorts.size() * sizeof(int), cudaMemcpyHostToDevice));

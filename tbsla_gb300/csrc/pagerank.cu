@@ -541,7 +541,7 @@ static tbsla_status_t pr_alloc(void **p, size_t bytes) {
 static int sweep_parts(const tbsla_matrix *A, bool fused) {
   if (!fused) return kAffineBlocks;
   int p = 0;
-  if (A->n_short > 0) p += short_grid(A->n_short, true);
+  p += short_parts_reducing(A);
   for (int c = 0; c < kGroupClasses; ++c) {
     const int count = A->item_class_start[c + 1] - A->item_class_start[c];
     if (count > 0) p += group_grid(count, kGroupLanes[c], true);

@@ -70,6 +70,21 @@ template <typename XT> inline XKeep xkeep_of(const tbsla_matrix *A) {
   return k;
 }
 
+// Reducing epilogues take the short list's tiny head (n_tiny rows of at most
+// kTinyRow entries) in warp tiles when the short-row kernel is the default.
+template <typename Epi> inline bool tiny_split(const tbsla_matrix *A) {
+  return Epi::kReduces && A->n_tiny > 0 && A->short_rows != nullptr && A->short_mode <= 0;
+}
+// the partial slots the short-row launches of a reducing epilogue write
+inline int short_parts_reducing(const tbsla_matrix *A) {
+  if (A->n_short == 0) return 0;
+  if (A->n_tiny > 0 && A->short_rows != nullptr && A->short_mode <= 0) {
+    const int rest = A->n_short - A->n_tiny;
+    return tiny_list_grid(A->n_tiny, true) + (rest > 0 ? short_grid(rest, true) : 0);
+  }
+  return short_grid(A->n_short, true);
+}
+
 // The staged kernel applies when every row is short (stage_cap > 0) and the
 // handle's stage mode (tbsla_matrix_tune) is on.
 inline bool stage_on(const tbsla_matrix *A) {
@@ -122,6 +137,20 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
     else
       csr_tiny_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(A->n_short, rowptr, colidx, vals, x, A->f_col,
                                                           xkeep_of<XT>(A), epi);
+  } else if (A->n_short > 0 && tiny_split<Epi>(A)) {
+    // the tiny head in warp tiles, the rest one thread per row
+    const int grid = tiny_list_grid(A->n_tiny, true);
+    epi.set_part_base(base);
+    base += grid;
+    csr_tiny_list_kernel<V, XT, Epi><<<grid, 256, 0, s>>>(A->short_rows, A->n_tiny, rowptr, colidx, vals, x,
+                                                          A->f_col, xkeep_of<XT>(A), epi);
+    const int rest = A->n_short - A->n_tiny;
+    if (rest > 0) {
+      epi.set_part_base(base);
+      base += short_grid(rest, true);
+      csr_short_kernel<V, XT, Epi><<<short_grid(rest, true), 256, 0, s>>>(
+          A->short_rows + A->n_tiny, rest, rowptr, colidx, vals, x, A->f_col, xkeep_of<XT>(A), epi);
+    }
   } else if (A->n_short > 0 && (A->short_mode == 2 || (A->short_mode < 0 && sizeof(V) == 8 && !Epi::kReduces &&
                                                        A->short_nnz >= (int64_t)kPairMinRow * A->n_short))) {
     // two lanes per row: twice the threads of the one-lane grid (reducing
