@@ -31,6 +31,8 @@
 
 namespace tbsla {
 
+tbsla_status_t csr_unsplit_tiny(tbsla_matrix *A);
+
 namespace {
 
 constexpr int kBandSamples = 4096;
@@ -200,6 +202,13 @@ tbsla_status_t build(tbsla_matrix *A, bool check_skew, bool *built) {
   va.clear(); va.shrink_to_fit();
   tbsla_matrix_t *B = nullptr;
   TB_TRY(tbsla_csr_create(n, n, 0, n, nrp.data(), nci.data(), nva.data(), A->stores, &B));
+  // rows are grouped by length here: one thread per short row over the
+  // whole list (the tiny-row tiles measured slower on this order)
+  const tbsla_status_t su = csr_unsplit_tiny(B);
+  if (su != TBSLA_OK) {
+    tbsla_matrix_destroy(B);
+    return su;
+  }
   B->x_keep = A->x_keep;
   B->x_keep_range = A->x_keep_range;
   B->short_mode = A->short_mode;
