@@ -132,3 +132,16 @@ def test_dropin_program_runs_on_gpu(gpu, tmp_path):
     run = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=600)
     fails = [l for l in run.stdout.splitlines() if l.startswith("FAIL")]
     assert run.returncode == 0 and "OK 0" in run.stdout, "\n".join(fails[:40]) + run.stderr[-2000:]
+
+
+def test_driver_programs_build(capi):
+    """build() compiles the driver programs (tbsla_gb300/apps) next to the
+    library; run without their required flags they print the reference
+    drivers' usage errors and exit 1 (no GPU needed for that)."""
+    from tbsla_gb300 import build
+    for name, msg in (("tbsla_perf", "A file format has to be given"),
+                      ("tbsla_page_rank", "A matrix file has to be given")):
+        exe = build.app_path(name)
+        assert os.path.exists(exe), exe
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 1 and msg in r.stderr, (name, r.returncode, r.stderr)
