@@ -61,9 +61,10 @@ X_BUFFERS = 4
 METRIC = "SpMV GB/s (% HBM peak); PageRank time-to-L1 1e-10, mixed vs FP64 GPU"
 WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # DRAM bytes (read + write) of one csr_pair_kernel launch on the 2^24
-# workload, from the ncu capture summarised in
+# workload with x rotated (the launch after one with another x), from the
+# one-kernel, one-launch ncu capture summarised in
 # profiles/csr_pair_kernel_cqmat_2p24.md
-NCU_TRAFFIC_BYTES = 3_952_693_597
+NCU_TRAFFIC_BYTES = 4_012_508_928
 
 
 def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):
