@@ -572,32 +572,31 @@ def batching_bench(capi, ppr_scale=22):
     sets = [rng.integers(0, n, int(np.exp(rng.uniform(0, np.log(100))))) for _ in range(k)]
     res = {"graph": f"R-MAT scale {ppr_scale}, 2^{ppr_scale + 4} draws, seed 1", "vectors": k, "tol": 1e-10}
     ref = torch.empty(k * n, dtype=torch.float64, device=dev)
-    for name, prec, tol in (("fp64", capi.F64, 1e-10), ("fp32", capi.F32, 1e-6)):
+    buf = torch.empty(k * n, dtype=torch.float64, device=dev)
+    # plain and Anderson-accelerated solves; FP32 iterates alone (to 1e-6),
+    # and FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined)
+    # to the FP64 tolerance; distances to the FP64 batched solve (itself at
+    # 1e-10)
+    for name, prec, tol, refined, accel in (("fp64", capi.F64, 1e-10, False, 0), ("fp32", capi.F32, 1e-6, False, 0),
+                                            ("fp32_refined", capi.F32, 1e-10, True, 0),
+                                            ("fp64_anderson", capi.F64, 1e-10, False, 1),
+                                            ("fp32_refined_anderson", capi.F32, 1e-10, True, 1)):
         t = G.autotune_ppr(k, prec)
-        buf = ref if prec == capi.F64 else torch.empty(k * n, dtype=torch.float64, device=dev)
+        out_buf = ref if name == "fp64" else buf
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        its, rs = capi.ppr_batched(G, sets, buf.data_ptr(), tol=tol, max_iter=1000, precision=prec)
+        its, rs = capi.ppr_batched(G, sets, out_buf.data_ptr(), tol=tol, max_iter=1000, precision=prec,
+                                   refined=refined, accel=accel)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         entry = {"tile": t.choice, "s": round(dt, 3), "ms_per_vector": round(dt * 1e3 / k, 3),
                  "sweeps_min_median_max": [int(its.min()), int(np.median(its)), int(its.max())],
                  "converged": int((rs < tol).sum())}
-        if prec == capi.F32:
+        if name != "fp64":
             entry["max_l1_vs_fp64"] = float((buf.view(k, n) - ref.view(k, n)).abs().sum(dim=1).max().item())
         res[name] = entry
-    # FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined) to
-    # the FP64 tolerance; distance to the FP64 batched solve (itself at 1e-10)
-    buf = torch.empty(k * n, dtype=torch.float64, device=dev)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    its, rs = capi.ppr_batched(G, sets, buf.data_ptr(), tol=1e-10, max_iter=1000, precision=capi.F32, refined=True)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    res["fp32_refined"] = {"s": round(dt, 3), "ms_per_vector": round(dt * 1e3 / k, 3),
-                           "sweeps_min_median_max": [int(its.min()), int(np.median(its)), int(its.max())],
-                           "converged": int((rs < 1e-10).sum()),
-                           "max_l1_vs_fp64": float((buf.view(k, n) - ref.view(k, n)).abs().sum(dim=1).max().item())}
+    for name in ("fp32_refined", "fp64_anderson", "fp32_refined_anderson"):
+        res[name + "_over_fp64_time"] = round(res[name]["s"] / res["fp64"]["s"], 3)
     del buf
     # one vector at a time (teleport form, same stopping rule)
     v = torch.zeros(n, dtype=torch.float64, device=dev)

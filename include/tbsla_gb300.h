@@ -444,10 +444,14 @@ tbsla_status_t tbsla_pagerank_adjoint(const tbsla_matrix_t *A, const tbsla_pager
  * stopped vectors are written out and the running ones repacked into as few
  * tiles as hold them; each result equals the vector solved alone bit for
  * bit.  p->precision: TBSLA_F64, or TBSLA_F32
- * (F32 value store and FP32 iterates).  d_out: n*k doubles, vector c at
- * d_out + c*n; iterations / residuals: k host entries each, or NULL.
- * Allocates its work buffers (2 n k values of the precision) per call.  No
- * reference counterpart. */
+ * (F32 value store and FP32 iterates).  p->accel = 1: each vector's solve is
+ * Anderson-accelerated (the combination of its last three sweep outputs
+ * whose residual combination is smallest, as in tbsla_pagerank; same
+ * stopping rule and fixed point, fewer sweeps).  d_out: n*k doubles, vector
+ * c at d_out + c*n; iterations / residuals: k host entries each, or NULL.
+ * Allocates its work buffers per call: 2 n k values of the precision, 7 n k
+ * with acceleration (iterate, three outputs, three residuals).  No reference
+ * counterpart. */
 tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_params_t *p, int k,
                                  const int *nodes, const int *offsets, int tile, double *d_out, int *iterations,
                                  double *residuals, void *stream);
@@ -457,7 +461,8 @@ tbsla_status_t tbsla_ppr_batched(const tbsla_matrix_t *A, const tbsla_pagerank_p
  * (stopped at max(p->tol, 1e-6)), then rounds of r = G(x) - x by one FP64
  * sweep of every vector; when every ||r_c||_1 < p->tol the result is G(x),
  * else the FP32 batched correction solve e = beta A e + beta (d.e) v_c + r_c
- * (from e = r_c, to ||e_j+1 - e_j||_1 < 1e-3 ||r_c||_1) and x += e, at most
+ * (from e = r_c, to ||e_j+1 - e_j||_1 < 1e-3 ||r_c||_1, 1e-4 with
+ * p->accel = 1, whose FP32 solves are accelerated) and x += e, at most
  * 8 rounds.  FP64 is used only for the residual sweeps, the L1 norms and the
  * update.  iterations: FP32 and FP64 sweeps together; residuals: the last
  * ||r_c||_1.  Allocates 2 n k doubles of work space per call (stream

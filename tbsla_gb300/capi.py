@@ -544,16 +544,17 @@ class Batch:
 
 
 def ppr_batched(A, seed_sets, d_out: int, beta=0.85, tol=1e-12, max_iter=10000, precision=F64, tile=0,
-                stream=None, check_every=0, refined=False):
+                stream=None, check_every=0, refined=False, accel=0):
     """k personalized PageRank vectors of A solved together; returns (iterations, residuals).
-    refined: FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined)."""
+    refined: FP32 sweeps with FP64 defect correction (tbsla_ppr_batched_refined);
+    accel: 1 for Anderson-accelerated solves (per vector)."""
     k = len(seed_sets)
     offsets = np.zeros(k + 1, np.int32)
     offsets[1:] = np.cumsum([len(s) for s in seed_sets])
     nodes = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int32) for s in seed_sets]), np.int32)
     its = np.zeros(k, np.int32)
     res = np.zeros(k, np.float64)
-    p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, precision, check_every)
+    p = PageRankParams(beta, tol, max_iter, PR_TELEPORT, precision, check_every, accel)
     fn = lib().tbsla_ppr_batched_refined if refined else lib().tbsla_ppr_batched
     check(fn(A.h, C.byref(p), k, _ptr(nodes), _ptr(offsets), tile, d_out, _ptr(its), _ptr(res), stream))
     return its, res

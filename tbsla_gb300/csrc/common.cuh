@@ -158,6 +158,10 @@ struct tbsla_matrix {
   int *transpose_perm = nullptr;
   // batched PageRank tile width chosen by tbsla_autotune_ppr (F64, F32); 0: none
   int ppr_tile[2] = {0, 0};
+  // batched PageRank work list built on first use (ppr_batch.cu; depends on
+  // the row structure only)
+  void *ppr_plan = nullptr;
+  void (*ppr_plan_free)(void *) = nullptr;
 
   // host-path staging
   cudaStream_t stream = nullptr;

@@ -225,6 +225,7 @@ static void free_handle(tbsla_matrix *A) {
   if (!A) return;
   cudaSetDevice(A->device);
   if (A->pr_work && A->pr_work_free) A->pr_work_free(A->pr_work);
+  if (A->ppr_plan && A->ppr_plan_free) A->ppr_plan_free(A->ppr_plan);
   if (A->pr_relabel) free_handle(A->pr_relabel);
   if (A->transpose) free_handle(A->transpose);
   for (void *p : A->values) if (p) cudaFree(p);

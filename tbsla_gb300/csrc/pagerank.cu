@@ -29,6 +29,7 @@
 #include <cstring>
 #include <vector>
 
+#include "anderson.cuh"
 #include "product.cuh"
 
 namespace tbsla {
@@ -331,13 +332,7 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
   case 13:    // residual dots of sweep k: r_k . r_k, r_k . r_{k-1}, r_k . r_{k-2}
   case 16: {  // the same for inner sweep k
     // shift the newest-first Gram matrix by one and add the new row
-    double(&gram)[3][3] = stage == 13 ? ctl->aa.gram : ctl->iaa.gram;
-    gram[2][2] = gram[1][1];
-    gram[1][2] = gram[2][1] = gram[0][1];
-    gram[1][1] = gram[0][0];
-    gram[0][0] = a;
-    gram[0][1] = gram[1][0] = b;
-    gram[0][2] = gram[2][0] = c;
+    aa_gram_push(stage == 13 ? ctl->aa.gram : ctl->iaa.gram, a, b, c);
     break;
   }
   case 17: {  // accelerated inner sweep k (as stage 3), its next-sweep term kept per slot
@@ -351,46 +346,16 @@ __global__ void __launch_bounds__(256) pr_finalize_kernel(const double *__restri
   }
 }
 
-// The Anderson step after sweep k (one thread): with q_j = r_{k-j}, minimise
-// || q_0 - g1 (q_0 - q_1) - g2 (q_1 - q_2) ||_2 over the available history
-// (normal equations from the Gram matrix), then the next input is
-// x_{k+1} = (1 - g1) g_k + (g1 - g2) g_{k-1} + g2 g_{k-2}.  The coefficients
-// sum to 1, and the next sweep's term is affine in its input, so it is the
-// same combination of the outputs' terms.  Ill-conditioned systems or large
-// coefficients fall back to fewer differences, down to the plain step
-// x_{k+1} = g_k.
+// The Anderson step after sweep k (one thread): the coefficients of the next
+// input in the last three outputs (aa_coefficients).  They sum to 1, and the
+// next sweep's term is affine in its input, so it is the same combination of
+// the outputs' terms.
 __global__ void pr_aa_solve_kernel(PrCtl *ctl, int inner) {
   if (*(volatile int *)(inner ? &ctl->inner_done : &ctl->done)) return;
   PrCtl::Aa &st = inner ? ctl->iaa : ctl->aa;
   const int k = (inner ? ctl->inner_iter : ctl->iter) - 1;  // the sweep just finished
-  int m = k < 2 ? k : 2;              // differences available
-  const double(&G)[3][3] = st.gram;
-  double g1 = 0, g2 = 0;
-  if (m == 2) {
-    const double a11 = G[0][0] - 2 * G[0][1] + G[1][1];
-    const double a12 = G[0][1] - G[0][2] - G[1][1] + G[1][2];
-    const double a22 = G[1][1] - 2 * G[1][2] + G[2][2];
-    const double b1 = G[0][0] - G[0][1], b2 = G[0][1] - G[0][2];
-    const double det = a11 * a22 - a12 * a12;
-    if (det > 1e-12 * a11 * a22 && a11 > 0 && a22 > 0) {
-      g1 = (b1 * a22 - b2 * a12) / det;
-      g2 = (a11 * b2 - a12 * b1) / det;
-    } else {
-      m = 1;
-    }
-    if (m == 2 && !(fabs(g1) < 8.0 && fabs(g2) < 8.0)) { g1 = g2 = 0; m = 1; }
-  }
-  if (m == 1) {
-    const double a11 = G[0][0] - 2 * G[0][1] + G[1][1], b1 = G[0][0] - G[0][1];
-    g1 = a11 > 0 ? b1 / a11 : 0.0;
-    g2 = 0;
-    if (!(fabs(g1) < 8.0)) g1 = 0;
-  }
-  const double c0 = 1.0 - g1, c1 = g1 - g2, c2 = g2;
-  st.coef[0] = c0;
-  st.coef[1] = c1;
-  st.coef[2] = c2;
-  st.m = (c1 != 0.0 || c2 != 0.0) ? (c2 != 0.0 ? 2 : 1) : 0;
+  st.m = aa_coefficients(st.gram, k < 2 ? k : 2, st.coef);
+  const double c0 = st.coef[0], c1 = st.coef[1], c2 = st.coef[2];
   const int s0 = k % 3, s1 = (k + 2) % 3, s2 = (k + 1) % 3;  // slots of g_k, g_{k-1}, g_{k-2}
   double add = c0 * st.add[s0];
   if (st.m >= 1) add += c1 * st.add[s1];

@@ -4,10 +4,20 @@
 // The k iterates are kept in tiles of KT columns (KT = 2, 4, 8, 16 or 32), each
 // tile row-major: tile t, row i holds X[i*KT + c] for its KT vectors, so the
 // gather of a column index brings all KT values in one contiguous segment.
-// A group of KT lanes sums a row, lane c for vector c: no cross-lane
-// reduction, every lane does useful multiply-adds.  Rows longer than
+// A group of G lanes sums a row, each lane VW consecutive vectors (16 bytes
+// of the tile row): no cross-lane reduction, every lane does useful
+// multiply-adds, and a warp sweeps 32 / G rows at once.  Rows longer than
 // kPprChunk entries are cut into chunks (partials + a fixup kernel) so that
-// hub rows of power-law graphs spread over many groups.
+// hub rows of power-law graphs spread over many groups.  The FP64 sweeps are
+// bound by the FP64 pipe as much as by their gathers (2 FMAs per clock per
+// SM: a 32-vector sweep of R-MAT 2^20, 5.2e8 FMAs, needs 0.83 ms of its
+// 1.35 ms).
+//
+// Anderson acceleration (p->accel = 1), per vector as in the one-vector
+// solve: the sweep writes its output g and residual r = g - x into rings of
+// three slots and sums r's dots with the two previous residuals; the
+// finalize solves each vector's 3x3 normal equations (aa_coefficients) and
+// the next input is the combination of the last three outputs.
 //
 // Per vector c with seed set P_c (v_c = 1/|P_c| on P_c):
 //   x_c <- beta A x_c + (beta d.x_c + 1 - beta) v_c,
@@ -28,6 +38,7 @@
 #include <cstring>
 #include <vector>
 
+#include "anderson.cuh"
 #include "product.cuh"
 
 namespace tbsla {
@@ -46,133 +57,352 @@ struct ColCtl {
 };
 struct TileCtl {
   int done, iter;  // iter: sweeps run on the tile (parity of the buffer holding it)
-  int pad[2];
+  int ran;         // the last sweep ran on the tile (it was not stopped before)
+  int pad;
+};
+// Anderson state of a column (accelerated solves): the next-sweep terms of
+// the last three outputs and their residuals' Gram matrix, newest first; the
+// weights of the next input in those outputs; residuals stored so far (0-3)
+struct ColAa {
+  double add[3];
+  double gram[3][3];
+  double coef[3];
+  int hist, m;
 };
 
-// Lane-column sums of a block for (resid, dmass) into partials[(part*KT+c)*2]
-template <int KT>
-__device__ __forceinline__ void block_columns(double r, double d, double *partials, int part) {
-  __shared__ double sh[8][32][2];
+// Lanes of the sweep kernels: each lane carries VW consecutive vectors (16
+// bytes of a tile row, or the whole row when it is narrower), so a row takes
+// G = KT / VW lanes and a warp sweeps 32 / G rows at once.
+template <typename T, int KT>
+struct PprLanes {
+  static constexpr int VW = KT * (int)sizeof(T) >= 16 ? 16 / (int)sizeof(T) : KT;
+  static constexpr int G = KT / VW;
+};
+template <typename T, int VW> struct PprVec;
+template <> struct PprVec<double, 2> { using type = double2; };
+template <> struct PprVec<float, 2> { using type = float2; };
+template <> struct PprVec<float, 4> { using type = float4; };
+
+template <typename T, int VW>
+__device__ __forceinline__ void ppr_ld(const T *p, T (&v)[VW]) {
+  using V = typename PprVec<T, VW>::type;
+  const V q = __ldg(reinterpret_cast<const V *>(p));
+  const T *s = reinterpret_cast<const T *>(&q);
+  #pragma unroll
+  for (int i = 0; i < VW; ++i) v[i] = s[i];
+}
+template <typename T, int VW>
+__device__ __forceinline__ void ppr_st(T *p, const T (&v)[VW]) {
+  using V = typename PprVec<T, VW>::type;
+  V q;
+  T *d = reinterpret_cast<T *>(&q);
+  #pragma unroll
+  for (int i = 0; i < VW; ++i) d[i] = v[i];
+  *reinterpret_cast<V *>(p) = q;
+}
+
+// Per-column sums of a block into partials[(part*KT + c)*NV + v], for the NV
+// values (resid, dangling mass, and with acceleration the residual dots
+// r.r, r.r_prev, r.r_prev2) that each lane holds for its VW columns (lane l
+// of a row group: columns l*VW .. l*VW+VW-1).  The warp's row groups are
+// summed by shuffles, then the warps in order.
+template <int KT, int VW, int NV>
+__device__ __forceinline__ void block_columns(double (&v)[NV][VW], double *partials, int part) {
+  constexpr int G = KT / VW;
+  __shared__ double sh[8][32][NV];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   #pragma unroll
-  for (int o = 16; o >= KT; o >>= 1) {
-    r += __shfl_down_sync(0xffffffffu, r, o);
-    d += __shfl_down_sync(0xffffffffu, d, o);
+  for (int o = 16; o >= G; o >>= 1) {
+    #pragma unroll
+    for (int j = 0; j < NV; ++j)
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) v[j][q] += __shfl_down_sync(0xffffffffu, v[j][q], o);
   }
-  if (lane < KT) {
-    sh[warp][lane][0] = r;
-    sh[warp][lane][1] = d;
+  if (lane < G) {
+    #pragma unroll
+    for (int j = 0; j < NV; ++j)
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) sh[warp][lane * VW + q][j] = v[j][q];
   }
   __syncthreads();
   if (threadIdx.x < KT) {
-    double a = 0, b = 0;
+    double a[NV];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) a[j] = 0;
     const int nw = blockDim.x >> 5;
-    for (int w = 0; w < nw; ++w) {
-      a += sh[w][threadIdx.x][0];
-      b += sh[w][threadIdx.x][1];
+    for (int w = 0; w < nw; ++w)
+      #pragma unroll
+      for (int j = 0; j < NV; ++j) a[j] += sh[w][threadIdx.x][j];
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) partials[((size_t)part * KT + threadIdx.x) * NV + j] = a[j];
+  }
+}
+
+// the residual ring of an accelerated sweep: r0 receives r = y - x, r1 / r2
+// hold the previous two sweeps' residuals
+template <typename T>
+struct PprRing {
+  T *r0;
+  const T *r1, *r2;
+};
+
+// A sweep's per-column constants for one lane's VW columns
+template <int VW>
+struct PprCols {
+  double tele[VW];  // teleport term added at seed rows
+  bool stopped[VW];
+  int hist[VW];  // accelerated: residuals stored before this sweep
+};
+template <int VW, bool AA>
+__device__ __forceinline__ void ppr_cols(PprCols<VW> &pc, int c, const ColCtl *col, const double *inv_size,
+                                         const ColAa *aa) {
+  #pragma unroll
+  for (int q = 0; q < VW; ++q) {
+    const ColCtl cc = col[c + q];
+    pc.stopped[q] = cc.done != 0;
+    pc.tele[q] = cc.add * inv_size[c + q];
+    pc.hist[q] = AA ? aa[c + q].hist : 0;
+  }
+}
+
+// The loads of a row's epilogue
+template <typename T, int VW, bool AA>
+struct PprRowIn {
+  T old[VW], rh[VW], r1[VW], r2[VW];
+  unsigned sd;
+  bool dm;
+};
+template <typename T, int VW, bool AA>
+__device__ __forceinline__ void ppr_row_in(PprRowIn<T, VW, AA> &in, int row, int KT, int c, const PprCols<VW> &pc,
+                                           const T *xo, const unsigned *seeds, const unsigned char *dmask,
+                                           const T *rhs, const PprRing<T> &ring) {
+  const size_t at = (size_t)row * KT + c;
+  ppr_ld<T, VW>(xo + at, in.old);
+  if (rhs) ppr_ld<T, VW>(rhs + at, in.rh);
+  in.sd = __ldg(seeds + row) >> c;
+  in.dm = __ldg(dmask + row) != 0;
+  if constexpr (AA) {
+    int h = 0;
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) h = max(h, pc.hist[q]);
+    if (h >= 1) ppr_ld<T, VW>(ring.r1 + at, in.r1);
+    if (h >= 2) ppr_ld<T, VW>(ring.r2 + at, in.r2);
+  }
+}
+
+// New values of one finished row for a lane's VW columns:
+//   y = beta acc + [seed row] tele + rhs (a stopped column keeps its value),
+// their L1 change and dangling mass; accelerated: r = y - x into the ring
+// and its dots with the previous residuals, summed per thread in shared
+// memory (dots[(j*VW + q)*256 + thread]: registers are the sweep's limit)
+template <typename T, int VW, int NV, bool AA>
+__device__ __forceinline__ void ppr_emit(int row, int KT, int c, const T (&acc)[VW], const PprCols<VW> &pc,
+                                         const PprRowIn<T, VW, AA> &in, T *xn, double beta, bool has_rhs,
+                                         const PprRing<T> &ring, double (&part)[NV][VW], double *dots) {
+  const size_t at = (size_t)row * KT + c;
+  T y[VW];
+  #pragma unroll
+  for (int q = 0; q < VW; ++q) {
+    if (pc.stopped[q]) {
+      y[q] = in.old[q];
+    } else {
+      double t = ((in.sd >> q) & 1u) ? pc.tele[q] : 0.0;
+      if (has_rhs) t += (double)in.rh[q];
+      y[q] = (T)((double)beta * (double)acc[q] + t);
+      part[0][q] += fabs((double)y[q] - (double)in.old[q]);
     }
-    partials[((size_t)part * KT + threadIdx.x) * 2 + 0] = a;
-    partials[((size_t)part * KT + threadIdx.x) * 2 + 1] = b;
+    if (in.dm) part[1][q] += (double)y[q];
+  }
+  ppr_st<T, VW>(xn + at, y);
+  if constexpr (AA) {
+    T r[VW];
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) r[q] = y[q] - in.old[q];
+    ppr_st<T, VW>(ring.r0 + at, r);
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) {
+      double *dq = dots + (size_t)q * 256 + threadIdx.x;
+      dq[0] += (double)r[q] * (double)r[q];
+      if (pc.hist[q] >= 1) dq[VW * 256] += (double)r[q] * (double)in.r1[q];
+      if (pc.hist[q] >= 2) dq[2 * VW * 256] += (double)r[q] * (double)in.r2[q];
+    }
   }
 }
 
-// y for one finished row (all KT lanes of the group)
-template <typename T, int KT>
-__device__ __forceinline__ void ppr_emit(int row, int c, T acc, const T *xo, T *xn, const unsigned *seeds,
-                                         const unsigned char *dmask, const ColCtl *col, const double *inv_size,
-                                         double beta, const T *rhs, double &r_acc, double &d_acc) {
-  const ColCtl cc = col[c];
-  const T old = xo[(size_t)row * KT + c];
-  T y;
-  if (cc.done) {
-    y = old;
-  } else {
-    double t = ((seeds[row] >> c) & 1u) ? cc.add * inv_size[c] : 0.0;
-    if (rhs) t += (double)rhs[(size_t)row * KT + c];
-    y = (T)((double)beta * (double)acc + t);
-    r_acc += fabs((double)y - (double)old);
-  }
-  if (dmask[row]) d_acc += (double)y;
-  xn[(size_t)row * KT + c] = y;
+// Resident blocks per SM the sweep kernel is compiled for (its register
+// budget, 64 registers): the sweeps are bound by the latency of their
+// gathers, and resident warps keep them in flight (R-MAT 2^22, 256 vectors,
+// FP64: 1 block per SM (144 registers) 1.77x the time of 4; 5 no faster)
+template <typename T, bool AA>
+constexpr int ppr_min_blocks() {
+  return 4;
 }
 
-// items: (row, begin, end, chunk slot or -1)
-template <typename T, int KT>
-__global__ void __launch_bounds__(256) ppr_spmm_kernel(const int4 *__restrict__ items, int n_items,
+// items: (row, begin, end, chunk slot or -1).  A row group of G lanes takes
+// an item, lane l its vectors l*VW .. l*VW+VW-1 (one 16-byte gather of the
+// tile row per entry); each vector's sum is one FMA per entry in stored order.
+template <typename T, int KT, bool AA>
+__global__ void __launch_bounds__(256, ppr_min_blocks<T, AA>()) ppr_spmm_kernel(const int4 *__restrict__ items, int n_items,
                                                       const int *__restrict__ colidx, const T *__restrict__ values,
                                                       const T *__restrict__ xo, T *__restrict__ xn,
                                                       const unsigned *__restrict__ seeds,
                                                       const unsigned char *__restrict__ dmask,
-                                                      const ColCtl *__restrict__ col,
+                                                      const ColCtl *__restrict__ col, const ColAa *__restrict__ aa,
                                                       const double *__restrict__ inv_size, double beta,
-                                                      const T *__restrict__ rhs, T *__restrict__ chunk_partials,
-                                                      double *partials, const TileCtl *tile) {
+                                                      const T *__restrict__ rhs, PprRing<T> ring,
+                                                      T *__restrict__ chunk_partials, double *partials,
+                                                      const TileCtl *tile) {
   if (*(volatile const int *)&tile->done) return;
-  const int c = threadIdx.x & (KT - 1);
-  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
-  double r_acc = 0, d_acc = 0;
-  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; g < n_items; g += ng) {
+  constexpr int VW = PprLanes<T, KT>::VW, G = PprLanes<T, KT>::G, NV = AA ? 5 : 2;
+  const int c = (threadIdx.x & (G - 1)) * VW;  // first vector of this lane
+  PprCols<VW> pc;
+  ppr_cols<VW, AA>(pc, c, col, inv_size, aa);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+  double part[NV][VW];
+  #pragma unroll
+  for (int j = 0; j < NV; ++j)
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) part[j][q] = 0;
+  __shared__ double dots[AA ? 3 * VW * 256 : 1];
+  if (AA)
+    for (int j = 0; j < 3 * VW; ++j) dots[j * 256 + threadIdx.x] = 0;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; g < n_items; g += ng) {
     const int4 it = items[g];
-    T acc = 0;
-    int e = it.y;
-    for (; e + 4 <= it.z; e += 4) {
-      const int c0 = __ldg(colidx + e), c1 = __ldg(colidx + e + 1), c2 = __ldg(colidx + e + 2),
-                c3 = __ldg(colidx + e + 3);
-      const T v0 = __ldg(values + e), v1 = __ldg(values + e + 1), v2 = __ldg(values + e + 2),
-              v3 = __ldg(values + e + 3);
-      const T x0 = __ldg(xo + (size_t)c0 * KT + c), x1 = __ldg(xo + (size_t)c1 * KT + c),
-              x2 = __ldg(xo + (size_t)c2 * KT + c), x3 = __ldg(xo + (size_t)c3 * KT + c);
-      acc = fma(v0, x0, acc);
-      acc = fma(v1, x1, acc);
-      acc = fma(v2, x2, acc);
-      acc = fma(v3, x3, acc);
+    T acc[VW];
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) acc[q] = 0;
+    // four entries per step, the last step predicated: a short row's
+    // gathers are all issued before its first multiply-add (R-MAT rows are
+    // mostly short, and one entry at a time chains index -> gather -> FMA)
+    for (int e = it.y; e < it.z; e += 4) {
+      const int rem = it.z - e;
+      int cj[4];
+      T vj[4], xj[4][VW];
+      #pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        cj[u] = u < rem ? __ldg(colidx + e + u) : 0;
+        vj[u] = u < rem ? __ldg(values + e + u) : T(0);
+      }
+      #pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u < rem) ppr_ld<T, VW>(xo + (size_t)cj[u] * KT + c, xj[u]);
+      #pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u < rem)
+          #pragma unroll
+          for (int q = 0; q < VW; ++q) acc[q] = fma(vj[u], xj[u][q], acc[q]);
     }
-    for (; e < it.z; ++e) acc = fma(__ldg(values + e), __ldg(xo + (size_t)__ldg(colidx + e) * KT + c), acc);
-    if (it.w >= 0) chunk_partials[(size_t)it.w * KT + c] = acc;
-    else ppr_emit<T, KT>(it.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, rhs, r_acc, d_acc);
+    if (it.w >= 0) {
+      ppr_st<T, VW>(chunk_partials + (size_t)it.w * KT + c, acc);
+    } else {
+      PprRowIn<T, VW, AA> in;
+      ppr_row_in<T, VW, AA>(in, it.x, KT, c, pc, xo, seeds, dmask, rhs, ring);
+      ppr_emit<T, VW, NV, AA>(it.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, part, dots);
+    }
   }
-  block_columns<KT>(r_acc, d_acc, partials, blockIdx.x);
+  if (AA)
+    #pragma unroll
+    for (int j = 0; j < 3; ++j)
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) part[AA ? 2 + j : 0][q] = dots[(j * VW + q) * 256 + threadIdx.x];
+  block_columns<KT, VW, NV>(part, partials, blockIdx.x);
 }
 
-// rows cut into chunks: crow[h] = (row, first slot), crow[n].y = total slots
-template <typename T, int KT>
+// rows cut into chunks: crow[h] = (row, first slot), crow[n].y = total slots;
+// the chunks' sums are added in order
+template <typename T, int KT, bool AA>
 __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__ crow, int n_crow,
                                                        const T *__restrict__ chunk_partials,
                                                        const T *__restrict__ xo, T *__restrict__ xn,
                                                        const unsigned *__restrict__ seeds,
                                                        const unsigned char *__restrict__ dmask,
-                                                       const ColCtl *__restrict__ col,
+                                                       const ColCtl *__restrict__ col, const ColAa *__restrict__ aa,
                                                        const double *__restrict__ inv_size, double beta,
-                                                       const T *__restrict__ rhs, double *partials, int part_base,
-                                                       const TileCtl *tile) {
+                                                       const T *__restrict__ rhs, PprRing<T> ring, double *partials,
+                                                       int part_base, const TileCtl *tile) {
   if (*(volatile const int *)&tile->done) return;
-  const int c = threadIdx.x & (KT - 1);
-  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
-  double r_acc = 0, d_acc = 0;
-  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; g < n_crow; g += ng) {
+  constexpr int VW = PprLanes<T, KT>::VW, G = PprLanes<T, KT>::G, NV = AA ? 5 : 2;
+  const int c = (threadIdx.x & (G - 1)) * VW;
+  PprCols<VW> pc;
+  ppr_cols<VW, AA>(pc, c, col, inv_size, aa);
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+  double part[NV][VW];
+  #pragma unroll
+  for (int j = 0; j < NV; ++j)
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) part[j][q] = 0;
+  __shared__ double dots[AA ? 3 * VW * 256 : 1];
+  if (AA)
+    for (int j = 0; j < 3 * VW; ++j) dots[j * 256 + threadIdx.x] = 0;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; g < n_crow; g += ng) {
     const int2 h = crow[g];
-    T acc = 0;
-    for (int s = h.y; s < crow[g + 1].y; ++s) acc += chunk_partials[(size_t)s * KT + c];
-    ppr_emit<T, KT>(h.x, c, acc, xo, xn, seeds, dmask, col, inv_size, beta, rhs, r_acc, d_acc);
+    T acc[VW];
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) acc[q] = 0;
+    for (int s = h.y; s < crow[g + 1].y; ++s) {
+      T p[VW];
+      ppr_ld<T, VW>(chunk_partials + (size_t)s * KT + c, p);
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) acc[q] += p[q];
+    }
+    PprRowIn<T, VW, AA> in;
+    ppr_row_in<T, VW, AA>(in, h.x, KT, c, pc, xo, seeds, dmask, rhs, ring);
+    ppr_emit<T, VW, NV, AA>(h.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, part, dots);
   }
-  block_columns<KT>(r_acc, d_acc, partials, part_base + blockIdx.x);
+  if (AA)
+    #pragma unroll
+    for (int j = 0; j < 3; ++j)
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) part[AA ? 2 + j : 0][q] = dots[(j * VW + q) * 256 + threadIdx.x];
+  block_columns<KT, VW, NV>(part, partials, part_base + blockIdx.x);
 }
 
-// per column: sum the parts in order, advance the column, then the tile
-template <int KT>
-__global__ void ppr_finalize_kernel(const double *__restrict__ partials, int nparts, ColCtl *col, TileCtl *tile,
-                                    double beta, double cst, int max_iter, int k_in_tile, int first) {
+// per column: sum the parts in order, advance the column, then the tile.
+// Accelerated: the new output's term and residual dots enter the column's
+// history and the weights of the next input are solved (aa_coefficients); a
+// column that stops takes its last output as it is.
+// 1024 threads: warp w sums the parts w, w + 32, ... in order, its lanes
+// reading each part's KT * NV values together; then the warps' sums are added
+// in order, and one thread per column advances it.
+template <int KT, bool AA>
+__global__ void __launch_bounds__(1024) ppr_finalize_kernel(const double *__restrict__ partials, int nparts,
+                                                           ColCtl *col, ColAa *aa, TileCtl *tile, double beta,
+                                                           double cst, int max_iter, int k_in_tile, int first) {
+  constexpr int NV = AA ? 5 : 2, W = KT * NV, PER = (W + 31) / 32;
+  __shared__ double sh[32][W];
   __shared__ int active;
   if (threadIdx.x == 0) active = 0;
   __syncthreads();
-  if (*(volatile int *)&tile->done) return;
+  if (*(volatile int *)&tile->done) {
+    if (threadIdx.x == 0) tile->ran = 0;
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double a[PER];
+  #pragma unroll
+  for (int i = 0; i < PER; ++i) a[i] = 0;
+  #pragma unroll 4
+  for (int p = warp; p < nparts; p += 32)
+    #pragma unroll
+    for (int i = 0; i < PER; ++i)
+      if (lane + 32 * i < W) a[i] += partials[(size_t)p * W + lane + 32 * i];
+  #pragma unroll
+  for (int i = 0; i < PER; ++i)
+    if (lane + 32 * i < W) sh[warp][lane + 32 * i] = a[i];
+  __syncthreads();
+  if (threadIdx.x < W) {
+    double t = 0;
+    for (int w = 0; w < 32; ++w) t += sh[w][threadIdx.x];
+    sh[0][threadIdx.x] = t;  // read only by this thread above
+  }
+  __syncthreads();
   const int c = threadIdx.x;
+  double v[NV];
+  if (c < KT)
+    #pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = sh[0][c * NV + j];
   if (c < KT) {
-    double r = 0, d = 0;
-    for (int p = 0; p < nparts; ++p) {
-      r += partials[((size_t)p * KT + c) * 2 + 0];
-      d += partials[((size_t)p * KT + c) * 2 + 1];
-    }
+    const double r = v[0], d = v[1];
     ColCtl &cc = col[c];
     if (first) {
       cc.add = beta * d + cst;  // initial vector: only the dangling mass is new
@@ -181,6 +411,25 @@ __global__ void ppr_finalize_kernel(const double *__restrict__ partials, int npa
       cc.resid = r;
       cc.add = beta * d + cst;
       cc.done = r < cc.tol || cc.iter >= max_iter;
+      if constexpr (AA) {
+        ColAa &st = aa[c];
+        st.add[2] = st.add[1];
+        st.add[1] = st.add[0];
+        st.add[0] = beta * d + cst;
+        aa_gram_push(st.gram, v[2], v[3], v[4]);
+        st.hist = min(st.hist + 1, 3);
+        if (cc.done) {
+          st.coef[0] = 1.0;
+          st.coef[1] = st.coef[2] = 0.0;
+          st.m = 0;
+        } else {
+          st.m = aa_coefficients(st.gram, st.hist - 1, st.coef);
+          double add = st.coef[0] * st.add[0];
+          if (st.m >= 1) add += st.coef[1] * st.add[1];
+          if (st.m >= 2) add += st.coef[2] * st.add[2];
+          cc.add = add;
+        }
+      }
     } else {
       cc.add = beta * d + cst;
     }
@@ -190,30 +439,71 @@ __global__ void ppr_finalize_kernel(const double *__restrict__ partials, int npa
   if (threadIdx.x == 0) {
     if (!first) tile->iter += 1;
     tile->done = active == 0;
+    tile->ran = 1;
   }
 }
 
-// x0 = v (seeds), dangling mass of x0 per column
+// accelerated: x = c0 g0 + c1 g1 + c2 g2 per column (g0 the newest output;
+// only the terms in use are read), after every sweep that ran on the tile
+// (also the one that stopped its last vector: x then takes its outputs)
 template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_combine_kernel(int n, const T *__restrict__ g0,
+                                                         const T *__restrict__ g1, const T *__restrict__ g2,
+                                                         T *__restrict__ x, const ColAa *__restrict__ aa,
+                                                         const TileCtl *tile) {
+  if (!*(volatile const int *)&tile->ran) return;
+  constexpr int VW = PprLanes<T, KT>::VW, G = PprLanes<T, KT>::G;
+  const int c = (threadIdx.x & (G - 1)) * VW;
+  T c0[VW], c1[VW], c2[VW];
+  int m[VW], mm = 0;
+  #pragma unroll
+  for (int q = 0; q < VW; ++q) {
+    const ColAa &st = aa[c + q];
+    c0[q] = (T)st.coef[0];
+    c1[q] = (T)st.coef[1];
+    c2[q] = (T)st.coef[2];
+    m[q] = st.m;
+    mm = max(mm, m[q]);
+  }
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; i < n; i += ng) {
+    const size_t at = (size_t)i * KT + c;
+    T a[VW], b[VW], e[VW], v[VW];
+    ppr_ld<T, VW>(g0 + at, a);
+    if (mm >= 1) ppr_ld<T, VW>(g1 + at, b);
+    if (mm >= 2) ppr_ld<T, VW>(g2 + at, e);
+    #pragma unroll
+    for (int q = 0; q < VW; ++q) {
+      v[q] = c0[q] * a[q];
+      if (m[q] >= 1) v[q] = fma(c1[q], b[q], v[q]);
+      if (m[q] >= 2) v[q] = fma(c2[q], e[q], v[q]);
+    }
+    ppr_st<T, VW>(x + at, v);
+  }
+}
+
+// x0 = v (seeds), dangling mass of x0 per column (partials of NV values per
+// column, the others 0)
+template <typename T, int KT, int NV>
 __global__ void __launch_bounds__(256) ppr_init_kernel(int n, const unsigned *__restrict__ seeds,
                                                       const unsigned char *__restrict__ dmask,
                                                       const double *__restrict__ inv_size, T *__restrict__ x,
                                                       double *partials) {
   const int c = threadIdx.x & (KT - 1);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
-  double d_acc = 0;
+  double part[NV][1] = {};
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; i < n; i += ng) {
     const T v = ((seeds[i] >> c) & 1u) ? (T)inv_size[c] : T(0);
     x[(size_t)i * KT + c] = v;
-    if (dmask[i]) d_acc += (double)v;
+    if (dmask[i]) part[1][0] += (double)v;
   }
-  block_columns<KT>(0.0, d_acc, partials, blockIdx.x);
+  block_columns<KT, 1, NV>(part, partials, blockIdx.x);
 }
 
 // x (one tile) from FP64 vectors in the original labels: vector vec[c] of
 // src (src + vec[c] * n) at tile row newid[u] (u when not relabelled);
 // columns with vec[c] < 0 get 0.  With partials: the dangling mass per column.
-template <typename T, int KT>
+template <typename T, int KT, int NV>
 __global__ void __launch_bounds__(256) ppr_load_kernel(int n, const double *__restrict__ src,
                                                       const int *__restrict__ vec, const int *__restrict__ newid,
                                                       const unsigned char *__restrict__ dmask, T *__restrict__ x,
@@ -221,14 +511,14 @@ __global__ void __launch_bounds__(256) ppr_load_kernel(int n, const double *__re
   const int c = threadIdx.x & (KT - 1);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / KT;
   const int v = vec[c];
-  double d_acc = 0;
+  double part[NV][1] = {};
   for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / KT; u < n; u += ng) {
     const int i = newid ? newid[u] : (int)u;
     const T val = v >= 0 ? (T)src[(size_t)v * n + u] : T(0);
     x[(size_t)i * KT + c] = val;
-    if (partials && dmask[i]) d_acc += (double)val;
+    if (partials && dmask[i]) part[1][0] += (double)val;
   }
-  if (partials) block_columns<KT>(0.0, d_acc, partials, blockIdx.x);
+  if (partials) block_columns<KT, 1, NV>(part, partials, blockIdx.x);
 }
 
 // dmask[j] = 1 when column j holds no nonzero value
@@ -270,28 +560,37 @@ __global__ void ppr_move_kernel(const T *__restrict__ src, T *__restrict__ dst, 
   }
 }
 
-// Options of one batched solve: by default x0 = v_c and the teleport form
-// x = beta A x + (beta d.x + 1 - beta) v_c.  A defect-correction solve passes
-// x0 = rhs = r_c and cst = 0: e = beta A e + beta (d.e) v_c + r_c.
-struct RunOpts {
-  const double *x0 = nullptr;   // start: vector c at x0 + src(c) * n (original labels), FP64
-  const double *rhs = nullptr;  // added to every sweep: rhs + src(c) * n
-  const int *src = nullptr;     // host: column of x0 / rhs for vector c (NULL: c)
-  double cst = -1.0;            // the constant of the teleport term (< 0: 1 - beta)
-  const double *tol = nullptr;  // host: stopping threshold per vector (NULL: p->tol)
-};
+// seeds[(slot / KT) * n + node] |= bit (slot % KT) for the (slot, node) pairs
+// of the seed sets (the array zeroed before)
+template <int KT>
+__global__ void ppr_seed_bits_kernel(unsigned *seeds, int n, const int2 *__restrict__ pairs, int npairs) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += gridDim.x * blockDim.x) {
+    const int2 q = pairs[i];
+    atomicOr(seeds + (size_t)(q.x / KT) * n + q.y, 1u << (q.x % KT));
+  }
+}
 
-template <typename T, int KT>
-tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std::vector<int> *newid_host,
-                         const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
-                         double *d_out, int *iters_out, double *resid_out, cudaStream_t s,
-                         const RunOpts &opt = RunOpts()) {
+// The work list of a handle's batched sweeps: rows, and rows longer than
+// kPprChunk entries cut into chunks; built once (it depends on the row
+// structure only) and kept on the handle.
+struct PprPlan {
+  int4 *items = nullptr;  // (row, begin, end, chunk slot or -1)
+  int2 *crow = nullptr;   // chunked rows: (row, first slot); crow[n_crow].y = slots
+  int n_items = 0, n_crow = 0, slots = 0;
+};
+void ppr_plan_free(void *q) {
+  PprPlan *P = static_cast<PprPlan *>(q);
+  if (P->items) cudaFree(P->items);
+  if (P->crow) cudaFree(P->crow);
+  delete P;
+}
+tbsla_status_t ppr_plan(const tbsla_matrix *Mc, const PprPlan **out) {
+  tbsla_matrix *M = const_cast<tbsla_matrix *>(Mc);
+  if (M->ppr_plan) {
+    *out = static_cast<const PprPlan *>(M->ppr_plan);
+    return TBSLA_OK;
+  }
   const int n = M->n_row;
-  const int64_t nnz = M->stored;
-  const T *values = static_cast<const T *>(M->values[std::is_same<T, double>::value ? 0 : 1]);
-  TB_CHECK(values, "the matrix lacks the %s value store", std::is_same<T, double>::value ? "F64" : "F32");
-  const int tiles = (k + KT - 1) / KT;
-  // work items: rows, and chunks of rows longer than kPprChunk
   std::vector<int> rp((size_t)n + 1);
   TB_CUDA(cudaMemcpy(rp.data(), M->idx0, ((size_t)n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
   std::vector<int4> items;
@@ -307,10 +606,91 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     crow.push_back(make_int2(r, slots));
     for (int e = a; e < b; e += kPprChunk) items.push_back(make_int4(r, e, std::min(e + kPprChunk, b), slots++));
   }
-  const int n_crow = (int)crow.size();
+  PprPlan *P = new PprPlan;
+  P->n_items = (int)items.size();
+  P->n_crow = (int)crow.size();
+  P->slots = slots;
   crow.push_back(make_int2(-1, slots));
-  // seeds: bit c of seeds[t*n + i] = row i is a seed of vector t*KT + c
-  std::vector<unsigned> seeds((size_t)tiles * n, 0u);
+  if (cudaMalloc((void **)&P->items, std::max<size_t>(items.size(), 1) * sizeof(int4)) != cudaSuccess ||
+      cudaMalloc((void **)&P->crow, crow.size() * sizeof(int2)) != cudaSuccess) {
+    cudaGetLastError();
+    ppr_plan_free(P);
+    return fail(TBSLA_ERR_OOM, "batched PageRank work list");
+  }
+  if ((!items.empty() &&
+       cudaMemcpy(P->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess) ||
+      cudaMemcpy(P->crow, crow.data(), crow.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess) {
+    ppr_plan_free(P);
+    return fail(TBSLA_ERR_CUDA, "batched PageRank work list upload");
+  }
+  M->ppr_plan = P;
+  M->ppr_plan_free = ppr_plan_free;
+  *out = P;
+  return TBSLA_OK;
+}
+
+// Accelerated repacking, in place: destination tile t of buf takes, per
+// column c, old slot map[c] (-1: zero).  The live vectors keep their order,
+// so every source of tile t lies in tile t or later; with the destination
+// tiles done in increasing order (one launch each) and the lanes of a warp
+// reading all their rows' sources before any of them writes (a row's sources
+// and destinations are in the same row, one warp's), nothing is overwritten
+// before it is read.
+template <typename T, int KT>
+__global__ void __launch_bounds__(256) ppr_compact_kernel(T *buf, int n, const int *__restrict__ map, int t) {
+  constexpr int VW = PprLanes<T, KT>::VW, G = PprLanes<T, KT>::G;
+  const int c = (threadIdx.x & (G - 1)) * VW;
+  int from[VW];
+  #pragma unroll
+  for (int q = 0; q < VW; ++q) from[q] = map[c + q];
+  const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
+  // warp-uniform loop: the warp's first row, then its lanes' rows
+  for (int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / G; i0 < n; i0 += ng) {
+    const int64_t i = i0 + (threadIdx.x & 31) / G;
+    T v[VW];
+    if (i < n) {
+      #pragma unroll
+      for (int q = 0; q < VW; ++q)
+        v[q] = from[q] < 0 ? T(0) : buf[((size_t)(from[q] / KT) * n + i) * KT + (from[q] % KT)];
+    }
+    __syncwarp();
+    if (i < n) ppr_st<T, VW>(buf + ((size_t)t * n + i) * KT + c, v);
+  }
+}
+
+// Options of one batched solve: by default x0 = v_c and the teleport form
+// x = beta A x + (beta d.x + 1 - beta) v_c.  A defect-correction solve passes
+// x0 = rhs = r_c and cst = 0: e = beta A e + beta (d.e) v_c + r_c.
+struct RunOpts {
+  const double *x0 = nullptr;   // start: vector c at x0 + src(c) * n (original labels), FP64
+  const double *rhs = nullptr;  // added to every sweep: rhs + src(c) * n
+  const int *src = nullptr;     // host: column of x0 / rhs for vector c (NULL: c)
+  double cst = -1.0;            // the constant of the teleport term (< 0: 1 - beta)
+  const double *tol = nullptr;  // host: stopping threshold per vector (NULL: p->tol)
+};
+
+// One batched solve in tiles of KT vectors; AA: Anderson-accelerated
+// (p->accel).  Plain sweeps ping-pong between two iterate buffers per tile;
+// accelerated ones read the iterate x, write the output g and residual r to
+// slot j % 3 of their rings (j counting the solve's sweeps), and the
+// combination of the last three outputs becomes the next x.
+template <typename T, int KT, bool AA>
+tbsla_status_t run_tiles_impl(const tbsla_matrix *M, const int *newid_dev, const std::vector<int> *newid_host,
+                              const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
+                              double *d_out, int *iters_out, double *resid_out, cudaStream_t s, const RunOpts &opt) {
+  constexpr int NV = AA ? 5 : 2;
+  constexpr int G = PprLanes<T, KT>::G;
+  const int n = M->n_row;
+  const int64_t nnz = M->stored;
+  const T *values = static_cast<const T *>(M->values[std::is_same<T, double>::value ? 0 : 1]);
+  TB_CHECK(values, "the matrix lacks the %s value store", std::is_same<T, double>::value ? "F64" : "F32");
+  const int tiles = (k + KT - 1) / KT;
+  const PprPlan *plan = nullptr;
+  TB_TRY(ppr_plan(M, &plan));
+  const int n_crow = plan->n_crow, slots = plan->slots;
+  // seeds: bit c of seeds[t*n + i] = row i is a seed of vector t*KT + c, set
+  // on the device from the (slot, node) pairs
+  std::vector<int2> pairs;
   std::vector<double> inv((size_t)tiles * KT, 0.0);
   std::vector<std::vector<int>> seed_sets((size_t)k);  // per vector, in the matrix's labels
   for (int c = 0; c < k; ++c) {
@@ -325,23 +705,32 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     }
     std::sort(dist.begin(), dist.end());
     dist.erase(std::unique(dist.begin(), dist.end()), dist.end());
-    for (int v : dist) seeds[(size_t)(c / KT) * n + v] |= 1u << (c % KT);
+    for (int v : dist) pairs.push_back(make_int2(c, v));
     inv[(size_t)c] = 1.0 / (double)dist.size();
   }
-  const int grid_mm = kStrideBlocks;
-  const int grid_fx = std::max(1, std::min((n_crow * KT + 255) / 256, 152 * 4));
+  // the sweep grid: two waves of the blocks that fit on the GPU at once (a
+  // grid-stride loop; one wave leaves SMs idle in its tail, more waves give
+  // the finalize more per-block partials to add: R-MAT 2^20, 64 vectors,
+  // 16 waves 1.47 ms per sweep + 0.75 ms finalize, 1 wave 1.58 + 0.05)
+  int sms = 0, per_sm = 0;
+  TB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, M->device));
+  TB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_spmm_kernel<T, KT, AA>, 256, 0));
+  const int grid_mm = std::max(1, 2 * sms * std::max(per_sm, 1));
+  const int grid_fx = std::max(1, std::min((n_crow * G + 255) / 256, sms * 4));
   const int grid_in = 152 * 4;
+  const int grid_vec = 152 * 8;  // streaming passes over a tile (combine, compaction)
   const int nparts = std::max(grid_mm + grid_fx, grid_in);
   // device buffers
   const size_t xbytes = (size_t)n * KT * sizeof(T);
   T *x[2] = {nullptr, nullptr};
+  T *g_ring[3] = {nullptr, nullptr, nullptr}, *r_ring[3] = {nullptr, nullptr, nullptr};
   T *chunk = nullptr;
-  int4 *d_items = nullptr;
-  int2 *d_crow = nullptr;
   unsigned *d_seeds = nullptr;
+  int2 *d_pairs = nullptr;
   unsigned char *dmask = nullptr;
   double *d_inv = nullptr, *partials = nullptr;
   ColCtl *d_col = nullptr;
+  ColAa *d_aa = nullptr;
   TileCtl *d_tile = nullptr;
   T *rhs_t[2] = {nullptr, nullptr};  // the right-hand side in the tiles' layout (ping-pong for repacking)
   int *d_vec = nullptr;              // per slot: the column of x0 / rhs it holds, or -1
@@ -357,20 +746,27 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     owned.push_back(*ptr);
   };
   alloc((void **)&x[0], (size_t)tiles * xbytes);
-  alloc((void **)&x[1], (size_t)tiles * xbytes);
+  if (AA) {
+    for (int j = 0; j < 3; ++j) {
+      alloc((void **)&g_ring[j], (size_t)tiles * xbytes);
+      alloc((void **)&r_ring[j], (size_t)tiles * xbytes);
+    }
+  } else {
+    alloc((void **)&x[1], (size_t)tiles * xbytes);
+  }
   alloc((void **)&chunk, (size_t)std::max(slots, 1) * KT * sizeof(T));
-  alloc((void **)&d_items, items.size() * sizeof(int4));
-  alloc((void **)&d_crow, crow.size() * sizeof(int2));
-  alloc((void **)&d_seeds, seeds.size() * sizeof(unsigned));
+  alloc((void **)&d_seeds, (size_t)tiles * n * sizeof(unsigned));
+  alloc((void **)&d_pairs, pairs.size() * sizeof(int2));
   alloc((void **)&dmask, (size_t)n);
   alloc((void **)&d_inv, inv.size() * sizeof(double));
-  alloc((void **)&partials, (size_t)tiles * nparts * KT * 2 * sizeof(double));
+  alloc((void **)&partials, (size_t)tiles * nparts * KT * NV * sizeof(double));
   alloc((void **)&d_col, (size_t)tiles * KT * sizeof(ColCtl));
+  alloc((void **)&d_aa, (size_t)tiles * KT * sizeof(ColAa));
   alloc((void **)&d_tile, (size_t)tiles * sizeof(TileCtl));
   alloc((void **)&d_vec, (size_t)tiles * KT * sizeof(int));
   if (opt.rhs) {
     alloc((void **)&rhs_t[0], (size_t)tiles * xbytes);
-    alloc((void **)&rhs_t[1], (size_t)tiles * xbytes);
+    if (!AA) alloc((void **)&rhs_t[1], (size_t)tiles * xbytes);
   }
   auto cleanup = [&]() {
     cudaStreamSynchronize(s);
@@ -386,18 +782,25 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     hcol[(size_t)c] = ColCtl{0.0, 0.0, c < k && opt.tol ? opt.tol[c] : p->tol, 0, c >= k ? 1 : 0};
     hvec[(size_t)c] = src_col(c < k ? c : -1);
   }
-  std::vector<TileCtl> htile((size_t)tiles, TileCtl{0, 0, {0, 0}});
+  // no history; the plain step
+  ColAa aa0;
+  std::memset(&aa0, 0, sizeof(aa0));
+  aa0.coef[0] = 1.0;
+  std::vector<ColAa> haa((size_t)tiles * KT, aa0);
+  std::vector<TileCtl> htile((size_t)tiles, TileCtl{0, 0, 0, 0});
   if (p->max_iter == 0)
     for (auto &tc : htile) tc.done = 1;
   cudaError_t e = cudaSuccess;
   auto up = [&](void *d, const void *h, size_t b) {
     if (e == cudaSuccess && b) e = cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, s);
   };
-  up(d_items, items.data(), items.size() * sizeof(int4));
-  up(d_crow, crow.data(), crow.size() * sizeof(int2));
-  up(d_seeds, seeds.data(), seeds.size() * sizeof(unsigned));
+  up(d_pairs, pairs.data(), pairs.size() * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_seeds, 0, (size_t)tiles * n * sizeof(unsigned), s);
+  if (e == cudaSuccess)
+    ppr_seed_bits_kernel<KT><<<152, 256, 0, s>>>(d_seeds, n, d_pairs, (int)pairs.size());
   up(d_inv, inv.data(), inv.size() * sizeof(double));
   up(d_col, hcol.data(), hcol.size() * sizeof(ColCtl));
+  up(d_aa, haa.data(), haa.size() * sizeof(ColAa));
   up(d_tile, htile.data(), htile.size() * sizeof(TileCtl));
   up(d_vec, hvec.data(), hvec.size() * sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(dmask, 1, (size_t)n, s);
@@ -405,18 +808,18 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   ppr_dangling_kernel<T><<<152 * 8, 256, 0, s>>>(M->idx1, values, nnz, dmask);
   const double beta = p->beta;
   for (int t = 0; t < tiles; ++t) {
-    double *pt = partials + (size_t)t * nparts * KT * 2;
+    double *pt = partials + (size_t)t * nparts * KT * NV;
     if (opt.x0)
-      ppr_load_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, opt.x0, d_vec + (size_t)t * KT, newid_dev, dmask,
-                                                     x[0] + (size_t)t * n * KT, pt);
+      ppr_load_kernel<T, KT, NV><<<grid_in, 256, 0, s>>>(n, opt.x0, d_vec + (size_t)t * KT, newid_dev, dmask,
+                                                         x[0] + (size_t)t * n * KT, pt);
     else
-      ppr_init_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, d_seeds + (size_t)t * n, dmask, d_inv + (size_t)t * KT,
-                                                     x[0] + (size_t)t * n * KT, pt);
+      ppr_init_kernel<T, KT, NV><<<grid_in, 256, 0, s>>>(n, d_seeds + (size_t)t * n, dmask,
+                                                         d_inv + (size_t)t * KT, x[0] + (size_t)t * n * KT, pt);
     if (opt.rhs)
-      ppr_load_kernel<T, KT><<<grid_in, 256, 0, s>>>(n, opt.rhs, d_vec + (size_t)t * KT, newid_dev, dmask,
-                                                     rhs_t[0] + (size_t)t * n * KT, nullptr);
-    ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, grid_in, d_col + (size_t)t * KT, d_tile + t, beta, cst,
-                                             p->max_iter, std::min(KT, k - t * KT), 1);
+      ppr_load_kernel<T, KT, NV><<<grid_in, 256, 0, s>>>(n, opt.rhs, d_vec + (size_t)t * KT, newid_dev, dmask,
+                                                         rhs_t[0] + (size_t)t * n * KT, nullptr);
+    ppr_finalize_kernel<KT, AA><<<1, 1024, 0, s>>>(pt, grid_in, d_col + (size_t)t * KT, d_aa + (size_t)t * KT,
+                                                 d_tile + t, beta, cst, p->max_iter, std::min(KT, k - t * KT), 1);
   }
   int rbase = 0;  // rhs_t[rbase] holds the current layout's right-hand side
   if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank init"); }
@@ -425,49 +828,68 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   // out and dropped; when the live vectors fit in fewer tiles they are
   // repacked (compaction), so a tile never keeps sweeping for one slow
   // vector while its other lanes idle.  All tiles of a layout sweep in step:
-  // the layout's iterates start in x[base] and sweep j reads x[(base+j)&1].
+  // plain, the layout's iterates start in x[base] and sweep j reads
+  // x[(base+j)&1]; accelerated, sweep number gk of the solve writes ring slot
+  // gk % 3.
   const int K = p->check_every > 0 ? p->check_every : 4;  // 4: R-MAT 2^22, 256 vectors, 3-9 % faster than 8
   int cur_tiles = tiles, base = 0;
+  int64_t gk = 0;
   std::vector<int> slot_vec((size_t)tiles * KT, -1);  // vector in each slot, -1 for none
   for (int c = 0; c < k; ++c) slot_vec[(size_t)c] = c;
   std::vector<TileCtl> htc((size_t)tiles);
   std::vector<ColCtl> hcc((size_t)tiles * KT);
+  std::vector<ColAa> hca((size_t)tiles * KT);
   int *d_map = nullptr;
   alloc((void **)&d_map, (size_t)tiles * KT * sizeof(int));
   if (st != TBSLA_OK) { cleanup(); return st; }
   std::vector<char> tile_live((size_t)tiles, 1);
   int phase = 0;
+  const size_t tstride = (size_t)n * KT;
   while (true) {
-    for (int k2 = 0; k2 < K; ++k2, ++phase) {
+    for (int k2 = 0; k2 < K; ++k2, ++phase, ++gk) {
+      const int w = (int)(gk % 3), w1 = (int)((gk + 2) % 3), w2 = (int)((gk + 1) % 3);
       for (int t = 0; t < cur_tiles; ++t) {
         if (!tile_live[(size_t)t]) continue;  // stopped in an earlier round
-        const T *xo = x[(base + phase) & 1] + (size_t)t * n * KT;
-        T *xn = x[(base + phase + 1) & 1] + (size_t)t * n * KT;
-        double *pt = partials + (size_t)t * nparts * KT * 2;
+        const size_t off = (size_t)t * tstride;
+        const T *xo = AA ? x[0] + off : x[(base + phase) & 1] + off;
+        T *xn = AA ? g_ring[w] + off : x[(base + phase + 1) & 1] + off;
+        PprRing<T> ring{AA ? r_ring[w] + off : nullptr, AA ? r_ring[w1] + off : nullptr,
+                        AA ? r_ring[w2] + off : nullptr};
+        double *pt = partials + (size_t)t * nparts * KT * NV;
         const unsigned *sd = d_seeds + (size_t)t * n;
         const ColCtl *cl = d_col + (size_t)t * KT;
+        const ColAa *ca = d_aa + (size_t)t * KT;
         const double *iv = d_inv + (size_t)t * KT;
-        const T *rh = opt.rhs ? rhs_t[rbase] + (size_t)t * n * KT : nullptr;
-        ppr_spmm_kernel<T, KT><<<grid_mm, 256, 0, s>>>(d_items, (int)items.size(), M->idx1, values, xo, xn, sd,
-                                                       dmask, cl, iv, beta, rh, chunk, pt, d_tile + t);
+        const T *rh = opt.rhs ? rhs_t[rbase] + off : nullptr;
+        ppr_spmm_kernel<T, KT, AA><<<grid_mm, 256, 0, s>>>(plan->items, plan->n_items, M->idx1, values, xo, xn,
+                                                           sd, dmask, cl, ca, iv, beta, rh, ring, chunk, pt,
+                                                           d_tile + t);
         if (n_crow)
-          ppr_fixup_kernel<T, KT><<<grid_fx, 256, 0, s>>>(d_crow, n_crow, chunk, xo, xn, sd, dmask, cl, iv, beta,
-                                                          rh, pt, grid_mm, d_tile + t);
-        ppr_finalize_kernel<KT><<<1, 32, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm, d_col + (size_t)t * KT,
-                                                 d_tile + t, beta, cst, p->max_iter, KT, 0);
+          ppr_fixup_kernel<T, KT, AA><<<grid_fx, 256, 0, s>>>(plan->crow, n_crow, chunk, xo, xn, sd, dmask, cl, ca,
+                                                              iv, beta, rh, ring, pt, grid_mm, d_tile + t);
+        ppr_finalize_kernel<KT, AA><<<1, 1024, 0, s>>>(pt, n_crow ? grid_mm + grid_fx : grid_mm,
+                                                     d_col + (size_t)t * KT, d_aa + (size_t)t * KT, d_tile + t,
+                                                     beta, cst, p->max_iter, KT, 0);
+        if (AA)
+          ppr_combine_kernel<T, KT><<<grid_vec, 256, 0, s>>>(n, g_ring[w] + off, g_ring[w1] + off,
+                                                            g_ring[w2] + off, x[0] + off, d_aa + (size_t)t * KT,
+                                                            d_tile + t);
       }
     }
     if (cudaMemcpyAsync(htc.data(), d_tile, (size_t)cur_tiles * sizeof(TileCtl), cudaMemcpyDeviceToHost, s) !=
             cudaSuccess ||
         cudaMemcpyAsync(hcc.data(), d_col, (size_t)cur_tiles * KT * sizeof(ColCtl), cudaMemcpyDeviceToHost, s) !=
             cudaSuccess ||
+        (AA && cudaMemcpyAsync(hca.data(), d_aa, (size_t)cur_tiles * KT * sizeof(ColAa), cudaMemcpyDeviceToHost,
+                               s) != cudaSuccess) ||
         cudaStreamSynchronize(s) != cudaSuccess) {
       cleanup();
       return fail(TBSLA_ERR_CUDA, "batched PageRank sweeps failed");
     }
     // write out and drop the vectors that stopped (a stopped vector is
-    // frozen: its tile's last iterate, x[(base + tile iter) & 1], holds it;
-    // a stopped tile's vectors have all stopped, or max_iter is 0)
+    // frozen: plain, its tile's last iterate, x[(base + tile iter) & 1],
+    // holds it; accelerated, x; a stopped tile's vectors have all stopped,
+    // or max_iter is 0)
     int live = 0, busy = 0;
     for (int t = 0; t < cur_tiles; ++t) {
       PprPicks pk;
@@ -487,7 +909,7 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
         }
       }
       if (pk.cnt) {
-        const T *xf = x[(base + htc[(size_t)t].iter) & 1] + (size_t)t * n * KT;
+        const T *xf = (AA ? x[0] : x[(base + htc[(size_t)t].iter) & 1]) + (size_t)t * tstride;
         ppr_pick_kernel<T, KT><<<152 * 8, 256, 0, s>>>(xf, n, newid_dev, pk, d_out);
       }
       tile_live[(size_t)t] = !htc[(size_t)t].done;
@@ -497,13 +919,16 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
     if (live == 0) break;
     const int need = (live + KT - 1) / KT;
     if (need < busy) {
-      // repack the live vectors into `need` tiles: their iterates (all in
-      // x[(base+phase)&1], every live tile having run all `phase` sweeps)
-      // move to the other buffer, which becomes the new layout's start
+      // repack the live vectors into `need` tiles (every live tile has run all
+      // `phase` sweeps of the layout): plain, their iterates (in
+      // x[(base+phase)&1]) move to the other buffer, which becomes the new
+      // layout's start; accelerated, the iterates, the rings and the
+      // right-hand side are compacted in place
       std::vector<int> map((size_t)need * KT, -1), nvec((size_t)need * KT, -1);
-      std::vector<unsigned> nseeds((size_t)need * n, 0u);
+      std::vector<int2> npairs;
       std::vector<double> ninv((size_t)need * KT, 0.0);
       std::vector<ColCtl> ncol((size_t)need * KT);
+      std::vector<ColAa> naa((size_t)need * KT, aa0);
       int q = 0;
       for (int t = 0; t < cur_tiles; ++t)
         for (int c = 0; c < KT; ++c) {
@@ -512,26 +937,38 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
           map[(size_t)q] = t * KT + c;
           nvec[(size_t)q] = v;
           ncol[(size_t)q] = hcc[(size_t)t * KT + c];
+          if (AA) naa[(size_t)q] = hca[(size_t)t * KT + c];
           ninv[(size_t)q] = inv[(size_t)t * KT + c];
-          for (int u : seed_sets[(size_t)v]) nseeds[(size_t)(q / KT) * n + u] |= 1u << (q % KT);
+          for (int u : seed_sets[(size_t)v]) npairs.push_back(make_int2(q, u));
           ++q;
         }
       for (size_t r = (size_t)q; r < ncol.size(); ++r) ncol[r] = ColCtl{0.0, 0.0, 0.0, 0, 1};
-      std::vector<TileCtl> ntile((size_t)need, TileCtl{0, 0, {0, 0}});
+      std::vector<TileCtl> ntile((size_t)need, TileCtl{0, 0, 0, 0});
       up(d_map, map.data(), map.size() * sizeof(int));
-      up(d_seeds, nseeds.data(), nseeds.size() * sizeof(unsigned));
+      up(d_pairs, npairs.data(), npairs.size() * sizeof(int2));  // no more pairs than at the start
+      if (e == cudaSuccess) e = cudaMemsetAsync(d_seeds, 0, (size_t)need * n * sizeof(unsigned), s);
+      if (e == cudaSuccess)
+        ppr_seed_bits_kernel<KT><<<152, 256, 0, s>>>(d_seeds, n, d_pairs, (int)npairs.size());
       up(d_inv, ninv.data(), ninv.size() * sizeof(double));
       up(d_col, ncol.data(), ncol.size() * sizeof(ColCtl));
+      if (AA) up(d_aa, naa.data(), naa.size() * sizeof(ColAa));
       up(d_tile, ntile.data(), ntile.size() * sizeof(TileCtl));
       if (e != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack: %s", cudaGetErrorString(e)); }
-      const int src = (base + phase) & 1;
-      ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(x[src], x[src ^ 1], n, d_map, need);
-      if (opt.rhs) {
-        ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(rhs_t[rbase], rhs_t[rbase ^ 1], n, d_map, need);
-        rbase ^= 1;
+      if (AA) {
+        T *bufs[8] = {x[0], g_ring[0], g_ring[1], g_ring[2], r_ring[0], r_ring[1], r_ring[2], rhs_t[0]};
+        for (int t = 0; t < need; ++t)
+          for (T *b : bufs)
+            if (b) ppr_compact_kernel<T, KT><<<grid_vec, 256, 0, s>>>(b, n, d_map + (size_t)t * KT, t);
+      } else {
+        const int src = (base + phase) & 1;
+        ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(x[src], x[src ^ 1], n, d_map, need);
+        if (opt.rhs) {
+          ppr_move_kernel<T, KT><<<152 * 8, 256, 0, s>>>(rhs_t[rbase], rhs_t[rbase ^ 1], n, d_map, need);
+          rbase ^= 1;
+        }
+        base = src ^ 1;
       }
       if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank repack"); }
-      base = src ^ 1;
       phase = 0;
       cur_tiles = need;
       slot_vec = nvec;
@@ -545,6 +982,18 @@ tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std:
   }
   cleanup();
   return TBSLA_OK;
+}
+
+template <typename T, int KT>
+tbsla_status_t run_tiles(const tbsla_matrix *M, const int *newid_dev, const std::vector<int> *newid_host,
+                         const tbsla_pagerank_params_t *p, int k, const int *nodes, const int *offsets,
+                         double *d_out, int *iters_out, double *resid_out, cudaStream_t s,
+                         const RunOpts &opt = RunOpts()) {
+  if (p->accel)
+    return run_tiles_impl<T, KT, true>(M, newid_dev, newid_host, p, k, nodes, offsets, d_out, iters_out,
+                                       resid_out, s, opt);
+  return run_tiles_impl<T, KT, false>(M, newid_dev, newid_host, p, k, nodes, offsets, d_out, iters_out, resid_out,
+                                      s, opt);
 }
 
 __global__ void ppr_sub_kernel(double *__restrict__ g, const double *__restrict__ x, int64_t n) {
@@ -562,7 +1011,8 @@ __global__ void ppr_add_kernel(double *__restrict__ x, const double *__restrict_
 // FP32 correction solve e = beta A e + beta (d.e) v_c + r_c from e = r_c to
 // ||e_j+1 - e_j||_1 < eta ||r_c||_1, and x += e.  Iterations: FP32 and FP64
 // sweeps together.
-constexpr double kRefineEta = 1e-3;     // inner tolerance relative to ||r_c||_1
+constexpr double kRefineEta = 1e-3;       // inner tolerance relative to ||r_c||_1
+constexpr double kRefineEtaAccel = 1e-4;  // the same for accelerated correction solves
 constexpr double kF32SolveFloor = 1e-6; // the FP32 solve's stopping threshold at least this
 constexpr int kRefineRounds = 8;
 
@@ -597,6 +1047,7 @@ tbsla_status_t run_refined(const tbsla_matrix *M, const int *nd, const std::vect
     // r = G(x) - x: one FP64 sweep from x (the sweep's L1 change is ||r_c||_1)
     tbsla_pagerank_params_t q64 = *p;
     q64.max_iter = 1;
+    q64.accel = 0;
     RunOpts o64;
     o64.x0 = d_out;
     TB_TRY((run_tiles<double, KT>(M, nd, nh, &q64, k, nodes, offsets, g, nullptr, res.data(), s, o64)));
@@ -613,7 +1064,7 @@ tbsla_status_t run_refined(const tbsla_matrix *M, const int *nd, const std::vect
     TB_CUDA(cudaGetLastError());
     // the correction, only as far as each vector still needs it
     for (int c = 0; c < k; ++c)
-      tolc[(size_t)c] = res[(size_t)c] < p->tol ? HUGE_VAL : kRefineEta * res[(size_t)c];
+      tolc[(size_t)c] = res[(size_t)c] < p->tol ? HUGE_VAL : (p->accel ? kRefineEtaAccel : kRefineEta) * res[(size_t)c];
     RunOpts oc;
     oc.x0 = g;
     oc.rhs = g;
