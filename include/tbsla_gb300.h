@@ -69,6 +69,9 @@ typedef struct {
   int stores;          /* TBSLA_STORE_* bits present                       */
   int64_t device_bytes;/* device memory held by the handle                 */
   int kernels;         /* kernel launches of one tbsla_spmv call           */
+  int slices;          /* CSR / row-sorted COO: 128-row slices of the sliced
+                          copy that plain products read (every row at most
+                          32 entries, at most 1/32 padding); 0 without one */
 } tbsla_matrix_info_t;
 
 /* ---------------------------------------------------------------- misc */
@@ -163,7 +166,8 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         range policy); 0 (default): a fraction of the
  *                         lines touched.
  *   TBSLA_TUNE_SHORT_ROWS the kernel for rows of at most 32 entries:
- *                         -1 (default) for plain products: when every row
+ *                         -1 (default) for plain products: the sliced copy
+ *                         (3) when the handle has one; else when every row
  *                         has at most 4 entries, warp tiles of 64 or 128
  *                         rows, lane l taking rows l, l+32, ... (one thread
  *                         per row's arithmetic, bit-identical to 0); else 2
@@ -176,7 +180,15 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         loads, rows summed from there in stored order
  *                         (bit-identical to 0); 2 two lanes per row, each
  *                         summing half the row in stored order, row = first
- *                         half + second half (rounds differently from 0).
+ *                         half + second half (rounds differently from 0);
+ *                         3 the sliced copy (tbsla_matrix_info_t.slices):
+ *                         a copy of the entries in 128-row slices, slot j
+ *                         of the slice's rows stored together, built at
+ *                         creation when every row has at most 32 entries,
+ *                         rows average 4 or more and the slices add at most
+ *                         1/32 padding slots; one thread per row summing in
+ *                         stored order (bit-identical to 0).  Without the
+ *                         copy, 3 acts as -1.
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)

@@ -38,7 +38,7 @@ class TbslaError(RuntimeError):
 class MatrixInfo(C.Structure):
     _fields_ = [("format", C.c_int), ("n_row", C.c_int), ("n_col", C.c_int), ("f_row", C.c_int),
                 ("f_col", C.c_int), ("rows", C.c_int), ("max_col", C.c_int), ("stored", C.c_int64),
-                ("stores", C.c_int), ("device_bytes", C.c_int64), ("kernels", C.c_int)]
+                ("stores", C.c_int), ("device_bytes", C.c_int64), ("kernels", C.c_int), ("slices", C.c_int)]
 
 
 class PageRankParams(C.Structure):

@@ -106,10 +106,19 @@ struct tbsla_matrix {
   // entries of the largest 32-row tile, a multiple of 16); 0 otherwise
   int stage_cap = 0;
   // short-row kernel (tbsla_matrix_tune): 0 one thread per row, 1 staged
-  // tiles (every row short), 2 two lanes per row, -1 (default) two lanes for
-  // plain products of FP64 values when short rows average at least
+  // tiles (every row short), 2 two lanes per row, 3 the sliced copy, -1
+  // (default) the sliced copy for plain products when it exists, else two
+  // lanes for plain products of FP64 values when short rows average at least
   // kPairMinRow entries, one thread per row otherwise
   int short_mode = -1;
+  // sliced copy of the entries (csr_sell_kernel): ELL layout, slot j of row
+  // r at j * sell_stride + r, sell_width slots, padding column -1; built when
+  // every row is short and padding adds little (csr_bins), kept for every
+  // value store (sell_vals[k] mirrors values[k])
+  int *sell_cols = nullptr;
+  void *sell_vals[3] = {nullptr, nullptr, nullptr};
+  int64_t sell_stride = 0;  // rows rounded up to a multiple of 128
+  int sell_width = 0;       // slots per row (the longest row); 0: no copy
   int4 *warp_items = nullptr;
   int n_warp_items = 0;
   int item_class_start[5] = {0, 0, 0, 0, 0};  // items of length class c: [start[c], start[c+1])

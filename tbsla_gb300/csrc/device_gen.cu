@@ -253,6 +253,8 @@ tbsla_status_t cqmat_stochastic_on_device(int format, int n_row, int n_col, int 
     // only the reduced stores were asked for: drop the F64 one
     cudaFree(A->values[0]);
     A->values[0] = nullptr;
+    if (A->sell_vals[0]) cudaFree(A->sell_vals[0]);
+    A->sell_vals[0] = nullptr;
     A->stores &= ~TBSLA_STORE_F64;
   }
   TB_CUDA(cudaDeviceSynchronize());

@@ -151,7 +151,29 @@ static tbsla_status_t upload_values(tbsla_matrix *A, const double *host, int64_t
   return TBSLA_OK;
 }
 
-// The F32 / BF16 stores of A recomputed from its F64 store
+// The sliced copies of A's value stores (csr_sell_kernel) from the stores
+static tbsla_status_t sell_refresh(tbsla_matrix *A, cudaStream_t s) {
+  if (!A->sell_width) return TBSLA_OK;
+  const int *rp = A->format == TBSLA_FMT_CSR ? A->idx0 : A->coo_rowptr;
+  const int grid = grid_for(A->rows, 256);
+  if (A->values[0])
+    sell_scatter_kernel<double><<<grid, 256, 0, s>>>(rp, A->sell_stride, A->rows,
+                                                     static_cast<const double *>(A->values[0]),
+                                                     static_cast<double *>(A->sell_vals[0]));
+  if (A->values[1])
+    sell_scatter_kernel<float><<<grid, 256, 0, s>>>(rp, A->sell_stride, A->rows,
+                                                    static_cast<const float *>(A->values[1]),
+                                                    static_cast<float *>(A->sell_vals[1]));
+  if (A->values[2])
+    sell_scatter_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(rp, A->sell_stride, A->rows,
+                                                            static_cast<const __nv_bfloat16 *>(A->values[2]),
+                                                            static_cast<__nv_bfloat16 *>(A->sell_vals[2]));
+  TB_CUDA(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// The F32 / BF16 stores of A recomputed from its F64 store (and the sliced
+// copies of all stores)
 tbsla_status_t rederive_stores(tbsla_matrix *A, cudaStream_t s) {
   const int64_t n = A->format == TBSLA_FMT_ELL ? (int64_t)A->rows_pad * A->max_col : A->stored;
   if (!A->values[0] || n == 0) return TBSLA_OK;
@@ -160,7 +182,7 @@ tbsla_status_t rederive_stores(tbsla_matrix *A, cudaStream_t s) {
   if (A->values[2])
     f64_to_bf16_kernel<<<grid_for(n, 256), 256, 0, s>>>(v, static_cast<__nv_bfloat16 *>(A->values[2]), n);
   TB_CUDA(cudaGetLastError());
-  return TBSLA_OK;
+  return sell_refresh(A, s);
 }
 
 tbsla_status_t transpose_refresh(tbsla_matrix *A, cudaStream_t s);
@@ -234,7 +256,8 @@ static void free_handle(tbsla_matrix *A) {
                   A->tile_start, A->tile_head_row, A->tile_head_val,
                   A->tile_tail_val, A->tile_emitted, A->tile_head_val32, A->tile_tail_val32,
                   A->dangling, A->pr_scratch, A->d_x, A->d_y, A->d_t, A->d_err, A->pr_newid, A->pr_out,
-                  A->transpose_perm, A->coo_rowptr};
+                  A->transpose_perm, A->coo_rowptr, A->sell_cols, A->sell_vals[0], A->sell_vals[1],
+                  A->sell_vals[2]};
   for (void *p : ptrs) if (p) cudaFree(p);
   if (A->stream) cudaStreamDestroy(A->stream);
   for (auto &e : A->pending_events) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -491,6 +514,31 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     if (!all_short && !shorts.empty()) {
       TB_TRY(alloc_n(A, &A->short_rows, (int64_t)shorts.size()));
       TB_CUDA(cudaMemcpy(A->short_rows, shorts.data(), shorts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    // the sliced copy (csr_sell_kernel): every row short, rows of at least 4
+    // entries on average, at most 1/32 more slots than entries
+    A->sell_width = 0;
+    if (all_short && rows >= kSellRows) {
+      int width = 0;
+      for (int r = 0; r < rows; ++r) width = std::max(width, rp[r + 1] - rp[r]);
+      const int64_t stride = ((int64_t)rows + kSellRows - 1) / kSellRows * kSellRows;
+      const int64_t total = stride * width;
+      const int64_t nnz = rp[rows];
+      if (nnz >= 4ll * rows && total <= nnz + nnz / 32) {
+        const int *rpd = A->format == TBSLA_FMT_CSR ? A->idx0 : A->coo_rowptr;
+        TB_TRY(alloc_n(A, &A->sell_cols, total));
+        TB_CUDA(cudaMemset(A->sell_cols, 0xff, (size_t)total * sizeof(int)));  // padding: column -1
+        sell_scatter_kernel<int><<<grid_for(rows, 256), 256>>>(rpd, stride, rows, A->idx1, A->sell_cols);
+        const size_t esz[3] = {8, 4, 2};
+        for (int k = 0; k < 3; ++k)
+          if (A->values[k]) {
+            TB_TRY(dev_alloc(A, &A->sell_vals[k], (size_t)total * esz[k]));
+            TB_CUDA(cudaMemset(A->sell_vals[k], 0, (size_t)total * esz[k]));
+          }
+        A->sell_stride = stride;
+        A->sell_width = width;
+        TB_TRY(sell_refresh(A, 0));
+      }
     }
     A->n_warp_items = (int)items.size();
     if (!items.empty()) {
@@ -784,8 +832,8 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
     A->pr_relabel_mode = (int)value;
     return TBSLA_OK;
   case TBSLA_TUNE_SHORT_ROWS:
-    TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0,
-             "short-row kernel mode %g not -1, 0, 1 or 2", value);
+    TB_CHECK(value == -1.0 || value == 0.0 || value == 1.0 || value == 2.0 || value == 3.0,
+             "short-row kernel mode %g not -1, 0, 1, 2 or 3", value);
     A->short_mode = (int)value;
     if (A->pr_relabel) A->pr_relabel->short_mode = (int)value;
     return TBSLA_OK;
@@ -873,6 +921,7 @@ tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *i
   default: k = (A->rows > 0 && A->cols > 0) ? 1 : 0; break;
   }
   info->kernels = k;
+  info->slices = A->sell_width ? (int)(A->sell_stride / kSellRows) : 0;
   return TBSLA_OK;
 }
 

@@ -103,6 +103,16 @@ template <typename V, typename XT, typename Epi> size_t csr_stage_setup(int cap)
   return csr_stage_smem<V>(cap);
 }
 
+// The sliced copy of the value store `vals` (csr_sell_kernel), when the
+// handle has one and plain products take it: the default short-row mode, or
+// mode 3
+template <typename V, typename Epi> inline const V *sell_vals_for(const tbsla_matrix *A, const V *vals) {
+  if (Epi::kReduces || !A->sell_width || !(A->short_mode == -1 || A->short_mode == 3)) return nullptr;
+  for (int k = 0; k < 3; ++k)
+    if (A->values[k] == static_cast<const void *>(vals)) return static_cast<const V *>(A->sell_vals[k]);
+  return nullptr;
+}
+
 // The direct CSR launches (row bins of the handle) over rowptr / colidx:
 // the CSR arrays of a CSR handle, or the derived row pointer of a row-sorted
 // COO handle.
@@ -112,6 +122,14 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
   using Acc = typename Epi::Acc;
   KernelTimer kt(A, s);
   int base = 0;
+  if (const V *sv = sell_vals_for<V, Epi>(A, vals)) {
+    // every row short, the ELL-layout copy: one warp per 128 rows
+    const int64_t threads = A->sell_stride / kSellRows * 32;
+    csr_sell_kernel<V, XT, Epi><<<(int)((threads + 255) / 256), 256, 0, s>>>(
+        A->sell_cols, sv, A->sell_stride, A->sell_width, x, A->f_col, A->rows, xkeep_of<XT>(A), epi);
+    kt.stop();
+    return TBSLA_OK;
+  }
   if (A->n_short > 0 && stage_on(A)) {
     // all rows short: the staged kernel (reducing epilogues: the same grid as
     // the short-row kernel, so that every partial slot is written)

@@ -544,3 +544,74 @@ def test_l2_persisting_setaside(gpu):
             m.tune(gpu.TUNE_X_L2_KEEP, keep)
             assert np.array_equal(m.spmv_host(x), y0)
     gpu.check(L.tbsla_set_l2_persisting(cur.value))
+
+
+def test_csr_sliced_copy(gpu, orc):
+    """The ELL-layout copy of short-row CSR / row-sorted COO handles
+    (csr_sell_kernel, TBSLA_TUNE_SHORT_ROWS -1 or 3): built only when every
+    row has at most 32 entries, rows average 4 or more and padding adds at
+    most 1/32 slots; each row summed in stored order, so every store's
+    product equals one thread per row (mode 0) bit for bit, and the oracle
+    within the FP64 bound; a_axpx through it; refreshed by set_values; rows
+    past `rows` and the output shift of COO unchanged."""
+    rng = np.random.default_rng(77)
+    n = 40000
+    lens = np.full(n, 12)
+    lens[rng.choice(n, 300, replace=False)] = 11  # a few padded slots
+    rp, ci, va = random_csr(rng, n, n, lens)
+    x = rng.uniform(-1, 1, n)
+    m = gpu.DeviceMatrix.csr(n, n, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16)
+    assert m.info().slices == (n + 127) // 128
+    o = orc.from_arrays("CSR", n, n, va, rp, ci)
+    so = orc.from_arrays("CSR", n, n, np.abs(va), rp, ci)
+    sc = so.spmv(np.abs(x))
+    y_sliced = m.spmv_host(x)
+    assert_close(y_sliced, o.spmv(x), sc, RTOL64, "sliced")
+    assert_close(m.a_axpx_host(x), o.a_axpx(x), so.spmv(sc + np.abs(x)), RTOL64, "sliced a_axpx")
+    for store, xt, tol in ((gpu.F32, np.float32, 2e-6), (gpu.BF16, np.float32, 2e-2)):
+        xs = Dev.of(gpu, x.astype(xt))
+        ys, y0 = Dev(gpu, n, np.float32), Dev(gpu, n, np.float32)
+        m.tune(gpu.TUNE_SHORT_ROWS, 3)
+        m.spmv_ex(store, gpu.F32, xs.ptr, gpu.F32, ys.ptr)
+        m.tune(gpu.TUNE_SHORT_ROWS, 0)
+        m.spmv_ex(store, gpu.F32, xs.ptr, gpu.F32, y0.ptr)
+        assert np.array_equal(ys.get(), y0.get()), store
+        assert_close(ys.get().astype(np.float64), o.spmv(x), sc, tol, f"sliced store {store}")
+    y_mode0 = m.spmv_host(x)
+    assert np.array_equal(y_sliced, y_mode0)
+    m.tune(gpu.TUNE_SHORT_ROWS, -1)
+    # new values: the copy follows
+    va2 = rng.uniform(-2, 2, va.size)
+    d_va2 = Dev.of(gpu, va2)
+    m.set_values(gpu.F64, d_va2.ptr)
+    o2 = orc.from_arrays("CSR", n, n, va2, rp, ci)
+    y2 = m.spmv_host(x)
+    m.tune(gpu.TUNE_SHORT_ROWS, 0)
+    assert np.array_equal(y2, m.spmv_host(x))
+    assert_close(y2, o2.spmv(x), orc.from_arrays("CSR", n, n, np.abs(va2), rp, ci).spmv(np.abs(x)), RTOL64,
+                 "sliced after set_values")
+    # the same entries as COO (row-sorted on the device): the copy as well,
+    # with the output shift of vect_incr
+    rows_of = np.repeat(np.arange(n, dtype=np.int32), np.diff(rp))
+    mc = gpu.DeviceMatrix.coo(n, n, rows_of, ci, va)
+    assert mc.info().slices > 0
+    oc = orc.from_arrays("COO", n, n, va, rows_of, ci)
+    for incr in (0, 3):
+        bound = np.zeros(n)
+        bound[incr:] = sc[: n - incr]
+        assert_close(mc.spmv_host(x, incr), oc.spmv(x, incr), bound, RTOL64, f"COO {incr}")
+    # rows below n_row (rows past them give 0)
+    part = n // 2 + 5
+    mp = gpu.DeviceMatrix.csr(n, n, rp[: part + 1], ci[: rp[part]], va[: rp[part]], rows=part)
+    assert mp.info().slices > 0
+    yp = mp.spmv_host(x)
+    assert np.array_equal(yp[part:], np.zeros(n - part)) and np.array_equal(yp[:part], y_sliced[:part])
+    # not built: a row longer than 32 entries; padding above 1/32; short rows
+    for bad in (np.r_[np.full(n - 1, 12), 40], np.r_[np.full(n // 2, 12), np.full(n - n // 2, 6)],
+                np.full(n, 3)):
+        rpb, cib, vab = random_csr(rng, n, n, bad)
+        mb = gpu.DeviceMatrix.csr(n, n, rpb, cib, vab)
+        assert mb.info().slices == 0
+        ob = orc.from_arrays("CSR", n, n, vab, rpb, cib)
+        assert_close(mb.spmv_host(x), ob.spmv(x), orc.from_arrays("CSR", n, n, np.abs(vab), rpb, cib).spmv(np.abs(x)),
+                     RTOL64, "no copy")
