@@ -64,7 +64,7 @@ WORKLOAD = "cqmat CSR FP64 SpMV n=2^{log2n} c=16 q=0.1 seed=0"
 # workload with x rotated (the launch after one with another x), from the
 # one-kernel, one-launch ncu capture summarised in
 # profiles/csr_sell_kernel_cqmat_2p24.md
-NCU_TRAFFIC_BYTES = 3_970_494_720
+NCU_TRAFFIC_BYTES = 3_898_083_328
 
 
 def csr_bytes(n_row, n_col, nnz, val_bytes=8, vec_bytes=8):

@@ -69,9 +69,9 @@ typedef struct {
   int stores;          /* TBSLA_STORE_* bits present                       */
   int64_t device_bytes;/* device memory held by the handle                 */
   int kernels;         /* kernel launches of one tbsla_spmv call           */
-  int slices;          /* CSR / row-sorted COO: 128-row slices of the sliced
-                          copy that plain products read (every row at most
-                          32 entries, at most 1/32 padding); 0 without one */
+  int slices;          /* CSR / row-sorted COO: 128-row tiles of the
+                          ELL-layout copy that plain F64 / F32 products read
+                          (TBSLA_TUNE_SHORT_ROWS 3); 0 without one         */
 } tbsla_matrix_info_t;
 
 /* ---------------------------------------------------------------- misc */
@@ -182,13 +182,21 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         summing half the row in stored order, row = first
  *                         half + second half (rounds differently from 0);
  *                         3 the sliced copy (tbsla_matrix_info_t.slices):
- *                         a copy of the entries in 128-row slices, slot j
- *                         of the slice's rows stored together, built at
- *                         creation when every row has at most 32 entries,
- *                         rows average 4 or more and the slices add at most
- *                         1/32 padding slots; one thread per row summing in
- *                         stored order (bit-identical to 0).  Without the
- *                         copy, 3 acts as -1.
+ *                         a copy of the entries in ELL layout (slot j of
+ *                         every row stored together, rows padded to a
+ *                         multiple of 128, padding marked by column -1),
+ *                         built at creation for matrices of at least 2^16
+ *                         rows when every row has at most 32 entries, rows
+ *                         average 4 or more and padding adds at most 1/32
+ *                         slots; kept for the F64 and F32 stores (BF16
+ *                         products read the CSR arrays); one thread per row
+ *                         summing in stored order (bit-identical to 0).
+ *                         Without the copy, 3 acts as -1.
+ *   TBSLA_TUNE_SELL_ROWS  rows per thread of the sliced copy's kernel: 1, 2
+ *                         or 4 (a warp takes 32, 64 or 128 rows); 0
+ *                         (default): 2, the fastest or within 3 % from 7e4
+ *                         to 1.6e7 rows (cqmat 2^24 FP64: 0.625 ms, 4 rows
+ *                         0.646 ms).
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)
@@ -209,7 +217,8 @@ typedef enum {
   TBSLA_TUNE_PR_RELABEL = 1,
   TBSLA_TUNE_X_L2_RANGE = 2,
   TBSLA_TUNE_SHORT_ROWS = 3,
-  TBSLA_TUNE_TC_SPLIT = 4
+  TBSLA_TUNE_TC_SPLIT = 4,
+  TBSLA_TUNE_SELL_ROWS = 5
 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);

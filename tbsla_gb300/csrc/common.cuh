@@ -113,12 +113,13 @@ struct tbsla_matrix {
   int short_mode = -1;
   // sliced copy of the entries (csr_sell_kernel): ELL layout, slot j of row
   // r at j * sell_stride + r, sell_width slots, padding column -1; built when
-  // every row is short and padding adds little (csr_bins), kept for every
-  // value store (sell_vals[k] mirrors values[k])
+  // every row is short and padding adds little (csr_bins), kept for the F64
+  // and F32 value stores (sell_vals[k] mirrors values[k]; [2] stays NULL)
   int *sell_cols = nullptr;
   void *sell_vals[3] = {nullptr, nullptr, nullptr};
   int64_t sell_stride = 0;  // rows rounded up to a multiple of 128
   int sell_width = 0;       // slots per row (the longest row); 0: no copy
+  int sell_rows = 0;        // rows per thread of csr_sell_kernel (1, 2, 4; 0: by size)
   int4 *warp_items = nullptr;
   int n_warp_items = 0;
   int item_class_start[5] = {0, 0, 0, 0, 0};  // items of length class c: [start[c], start[c+1])

@@ -550,43 +550,45 @@ __global__ void csr_chunk_fixup_kernel(const int2 *__restrict__ huge, int n_huge
 // ------------------------------------------------------- sliced copy
 // Every row short, few padded slots: a copy of the entries in ELL layout,
 // slot j of every row stored together (rows padded to a multiple of 128,
-// width = the longest row; padded slots hold column -1).  One warp per 128
-// rows, lane l taking rows l, l + 32, l + 64, l + 96: each slot's indices and
-// values are four fully used 128-entry runs, and the gathers of neighbouring
-// rows' band entries fall on neighbouring addresses.  Padded slots are
-// skipped.  Each row is summed in its stored order, one FMA per entry (the
+// width = the longest row; padded slots hold column -1).  One warp per 32 R
+// rows, lane l taking rows l, l + 32, ...: each slot's indices and values
+// are R fully used 32-entry runs, and the gathers of neighbouring rows' band
+// entries fall on neighbouring addresses.  Padded slots are skipped.  R = 2
+// by default (two independent loads per slot and thread).  Each row is summed in its stored order, one FMA per entry (the
 // order of MatrixCSR::Ax, src/cpp/matrix/MatrixCSR.cpp:133-139).
 constexpr int kSellRows = 128;
 
-template <typename V, typename XT, typename Epi>
+template <int R, typename V, typename XT, typename Epi>
 __global__ void __launch_bounds__(256) csr_sell_kernel(const int *__restrict__ cols, const V *__restrict__ vals,
                                                       int64_t stride, int width, const XT *__restrict__ x,
                                                       int f_col, int rows, XKeep x_keep, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
-  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * kSellRows;
+  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * (32 * R);
   const int lane = threadIdx.x & 31;
   typename Epi::State es{};
   if (base < rows) {
     const uint64_t keep = policy_keep(x_keep, x);
     const int r0 = (int)base + lane;
-    Acc a[4] = {0, 0, 0, 0};
+    Acc a[R];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) a[q] = 0;
     #pragma unroll 4
     for (int j = 0; j < width; ++j) {
       const size_t off = (size_t)j * stride + r0;
-      int c[4];
-      V v[4];
+      int c[R];
+      V v[R];
       #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < R; ++q) {
         c[q] = ld_ell<false>(cols + off + 32 * q);
         v[q] = ld_ell<false>(vals + off + 32 * q);
       }
       #pragma unroll
-      for (int q = 0; q < 4; ++q)
+      for (int q = 0; q < R; ++q)
         if (c[q] >= 0) a[q] = fma_acc(to_acc(v[q], Acc()), to_acc(ld_keep(x + (c[q] - f_col), keep), Acc()), a[q]);
     }
     #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < R; ++q)
       if (r0 + 32 * q < rows) epi.emit(r0 + 32 * q, a[q], es);
   }
   epi.block_done(es, blockIdx.x);

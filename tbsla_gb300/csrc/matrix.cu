@@ -164,10 +164,6 @@ static tbsla_status_t sell_refresh(tbsla_matrix *A, cudaStream_t s) {
     sell_scatter_kernel<float><<<grid, 256, 0, s>>>(rp, A->sell_stride, A->rows,
                                                     static_cast<const float *>(A->values[1]),
                                                     static_cast<float *>(A->sell_vals[1]));
-  if (A->values[2])
-    sell_scatter_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(rp, A->sell_stride, A->rows,
-                                                            static_cast<const __nv_bfloat16 *>(A->values[2]),
-                                                            static_cast<__nv_bfloat16 *>(A->sell_vals[2]));
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
 }
@@ -518,7 +514,7 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
     // the sliced copy (csr_sell_kernel): every row short, rows of at least 4
     // entries on average, at most 1/32 more slots than entries
     A->sell_width = 0;
-    if (all_short && rows >= kSellRows) {
+    if (all_short && rows >= (1 << 16)) {
       int width = 0;
       for (int r = 0; r < rows; ++r) width = std::max(width, rp[r + 1] - rp[r]);
       const int64_t stride = ((int64_t)rows + kSellRows - 1) / kSellRows * kSellRows;
@@ -529,8 +525,8 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
         TB_TRY(alloc_n(A, &A->sell_cols, total));
         TB_CUDA(cudaMemset(A->sell_cols, 0xff, (size_t)total * sizeof(int)));  // padding: column -1
         sell_scatter_kernel<int><<<grid_for(rows, 256), 256>>>(rpd, stride, rows, A->idx1, A->sell_cols);
-        const size_t esz[3] = {8, 4, 2};
-        for (int k = 0; k < 3; ++k)
+        const size_t esz[2] = {8, 4};
+        for (int k = 0; k < 2; ++k)  // F64 and F32 stores (BF16 products read the CSR arrays)
           if (A->values[k]) {
             TB_TRY(dev_alloc(A, &A->sell_vals[k], (size_t)total * esz[k]));
             TB_CUDA(cudaMemset(A->sell_vals[k], 0, (size_t)total * esz[k]));
@@ -841,6 +837,11 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
     TB_CHECK(value == 0.0 || value == 1.0 || value == 2.0 || value == 4.0 || value == 8.0 || value == 16.0,
              "tensor-core K split %g not 0, 1, 2, 4, 8 or 16", value);
     A->tc_split = (int)value;
+    return TBSLA_OK;
+  case TBSLA_TUNE_SELL_ROWS:
+    TB_CHECK(value == 0.0 || value == 1.0 || value == 2.0 || value == 4.0,
+             "rows per thread %g not 0, 1, 2 or 4", value);
+    A->sell_rows = (int)value;
     return TBSLA_OK;
   case TBSLA_TUNE_X_L2_RANGE:
     TB_CHECK(value == 0.0 || value == 1.0, "x L2 range mode %g not 0 or 1", value);

@@ -103,11 +103,20 @@ template <typename V, typename XT, typename Epi> size_t csr_stage_setup(int cap)
   return csr_stage_smem<V>(cap);
 }
 
+// Rows per thread of csr_sell_kernel: the handle's setting, else 2 (cqmat
+// 7e4 to 1.6e7 rows, c 8 to 32, FP32 and FP64: 2 the fastest or within 3 %;
+// the 2^24 FP64 product 0.625 ms against 0.646 with 4 and more with 1)
+inline int sell_rows_per_thread(const tbsla_matrix *A) {
+  return A->sell_rows > 0 ? A->sell_rows : 2;
+}
+
 // The sliced copy of the value store `vals` (csr_sell_kernel), when the
 // handle has one and plain products take it: the default short-row mode, or
-// mode 3
+// mode 3; F64 and F32 stores (BF16 slots load 64 bytes per warp instruction:
+// cqmat 2^24 0.366 ms against 0.334 with one thread per row)
 template <typename V, typename Epi> inline const V *sell_vals_for(const tbsla_matrix *A, const V *vals) {
   if (Epi::kReduces || !A->sell_width || !(A->short_mode == -1 || A->short_mode == 3)) return nullptr;
+  if (sizeof(V) < 4) return nullptr;  // BF16: the copy is not kept
   for (int k = 0; k < 3; ++k)
     if (A->values[k] == static_cast<const void *>(vals)) return static_cast<const V *>(A->sell_vals[k]);
   return nullptr;
@@ -123,10 +132,19 @@ tbsla_status_t launch_csr_direct(const tbsla_matrix *A, const int *rowptr, const
   KernelTimer kt(A, s);
   int base = 0;
   if (const V *sv = sell_vals_for<V, Epi>(A, vals)) {
-    // every row short, the ELL-layout copy: one warp per 128 rows
-    const int64_t threads = A->sell_stride / kSellRows * 32;
-    csr_sell_kernel<V, XT, Epi><<<(int)((threads + 255) / 256), 256, 0, s>>>(
-        A->sell_cols, sv, A->sell_stride, A->sell_width, x, A->f_col, A->rows, xkeep_of<XT>(A), epi);
+    // every row short, the ELL-layout copy: one warp per 32 R rows
+    const int R = sell_rows_per_thread(A);
+    const int64_t threads = A->sell_stride / (32 * R) * 32;
+    const int grid = (int)((threads + 255) / 256);
+    if (R == 4)
+      csr_sell_kernel<4, V, XT, Epi><<<grid, 256, 0, s>>>(A->sell_cols, sv, A->sell_stride, A->sell_width, x,
+                                                          A->f_col, A->rows, xkeep_of<XT>(A), epi);
+    else if (R == 2)
+      csr_sell_kernel<2, V, XT, Epi><<<grid, 256, 0, s>>>(A->sell_cols, sv, A->sell_stride, A->sell_width, x,
+                                                          A->f_col, A->rows, xkeep_of<XT>(A), epi);
+    else
+      csr_sell_kernel<1, V, XT, Epi><<<grid, 256, 0, s>>>(A->sell_cols, sv, A->sell_stride, A->sell_width, x,
+                                                          A->f_col, A->rows, xkeep_of<XT>(A), epi);
     kt.stop();
     return TBSLA_OK;
   }

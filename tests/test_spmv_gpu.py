@@ -553,9 +553,11 @@ def test_csr_sliced_copy(gpu, orc):
     most 1/32 slots; each row summed in stored order, so every store's
     product equals one thread per row (mode 0) bit for bit, and the oracle
     within the FP64 bound; a_axpx through it; refreshed by set_values; rows
-    past `rows` and the output shift of COO unchanged."""
+    past `rows` and the output shift of COO unchanged; every rows-per-thread
+    setting (TBSLA_TUNE_SELL_ROWS) gives the same bits; no copy below 2^16
+    rows."""
     rng = np.random.default_rng(77)
-    n = 40000
+    n = 70000
     lens = np.full(n, 12)
     lens[rng.choice(n, 300, replace=False)] = 11  # a few padded slots
     rp, ci, va = random_csr(rng, n, n, lens)
@@ -580,6 +582,10 @@ def test_csr_sliced_copy(gpu, orc):
     y_mode0 = m.spmv_host(x)
     assert np.array_equal(y_sliced, y_mode0)
     m.tune(gpu.TUNE_SHORT_ROWS, -1)
+    for rows_per_thread in (1, 2, 4):
+        m.tune(gpu.TUNE_SELL_ROWS, rows_per_thread)
+        assert np.array_equal(m.spmv_host(x), y_mode0), rows_per_thread
+    m.tune(gpu.TUNE_SELL_ROWS, 0)
     # new values: the copy follows
     va2 = rng.uniform(-2, 2, va.size)
     d_va2 = Dev.of(gpu, va2)
@@ -590,18 +596,24 @@ def test_csr_sliced_copy(gpu, orc):
     assert np.array_equal(y2, m.spmv_host(x))
     assert_close(y2, o2.spmv(x), orc.from_arrays("CSR", n, n, np.abs(va2), rp, ci).spmv(np.abs(x)), RTOL64,
                  "sliced after set_values")
-    # the same entries as COO (row-sorted on the device): the copy as well,
-    # with the output shift of vect_incr
-    rows_of = np.repeat(np.arange(n, dtype=np.int32), np.diff(rp))
-    mc = gpu.DeviceMatrix.coo(n, n, rows_of, ci, va)
+    # below 2^16 rows: no copy
+    small = gpu.DeviceMatrix.csr(50000, n, rp[:50001], ci[: rp[50000]], va[: rp[50000]])
+    assert small.info().slices == 0
+    # the same entries as COO (row-sorted on the device), the last three rows
+    # empty so that the output shift of vect_incr stays inside y (the
+    # reference's Ax writes r[row + vect_incr] unchecked): the copy as well
+    keep = rp[n - 3]
+    rows_of = np.repeat(np.arange(n, dtype=np.int32), np.diff(rp))[:keep]
+    mc = gpu.DeviceMatrix.coo(n, n, rows_of, ci[:keep], va[:keep])
     assert mc.info().slices > 0
-    oc = orc.from_arrays("COO", n, n, va, rows_of, ci)
+    oc = orc.from_arrays("COO", n, n, va[:keep], rows_of, ci[:keep])
+    sc3 = orc.from_arrays("COO", n, n, np.abs(va[:keep]), rows_of, ci[:keep]).spmv(np.abs(x))
     for incr in (0, 3):
         bound = np.zeros(n)
-        bound[incr:] = sc[: n - incr]
+        bound[incr:] = sc3[: n - incr]
         assert_close(mc.spmv_host(x, incr), oc.spmv(x, incr), bound, RTOL64, f"COO {incr}")
     # rows below n_row (rows past them give 0)
-    part = n // 2 + 5
+    part = n - 1003
     mp = gpu.DeviceMatrix.csr(n, n, rp[: part + 1], ci[: rp[part]], va[: rp[part]], rows=part)
     assert mp.info().slices > 0
     yp = mp.spmv_host(x)
