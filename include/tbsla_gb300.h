@@ -192,11 +192,12 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         products read the CSR arrays); one thread per row
  *                         summing in stored order (bit-identical to 0).
  *                         Without the copy, 3 acts as -1.
- *   TBSLA_TUNE_SELL_ROWS  rows per thread of the sliced copy's kernel: 1, 2
- *                         or 4 (a warp takes 32, 64 or 128 rows); 0
- *                         (default): 2, the fastest or within 3 % from 7e4
- *                         to 1.6e7 rows (cqmat 2^24 FP64: 0.625 ms, 4 rows
- *                         0.646 ms).
+ *   TBSLA_TUNE_SELL_ROWS  rows per thread of the sliced copy's kernel and of
+ *                         the ELL warp tiles: 1, 2 or 4 (a warp takes 32, 64
+ *                         or 128 rows); 0 (default): 2, the fastest or within
+ *                         3 % from 7e4 to 1.6e7 rows (cqmat 2^24 FP64: CSR
+ *                         copy 0.625 ms, 4 rows 0.646 ms; ELL 0.629 against
+ *                         0.649 ms).  Results do not depend on it.
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)

@@ -270,15 +270,30 @@ tbsla_status_t launch_product(const tbsla_matrix *A, const V *vals, const XT *x,
       const bool cs = A->x_extent * (int64_t)sizeof(XT) <= (64ll << 20);
       KernelTimer kt(A, s);
       if (A->csr_variant == 0) {
-        // warp tiles of 128 rows (the default)
-        const int64_t threads = ((int64_t)A->rows + 127) / 128 * 32;
+        // warp tiles of 32 R rows (the default), R rows per thread
+        // (TBSLA_TUNE_SELL_ROWS)
+        const int R = sell_rows_per_thread(A);
+        const int64_t threads = ((int64_t)A->rows + 32 * R - 1) / (32 * R) * 32;
         const int grid = (int)((threads + 255) / 256);
-        if (cs)
-          ell_warp_kernel<V, XT, Epi, true><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows, A->rows_pad,
-                                                                 A->max_col, xkeep_of<XT>(A), epi);
+        const XKeep k = xkeep_of<XT>(A);
+        if (cs && R == 4)
+          ell_warp_kernel<V, XT, Epi, true, 4><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                    A->rows_pad, A->max_col, k, epi);
+        else if (cs && R == 2)
+          ell_warp_kernel<V, XT, Epi, true, 2><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                    A->rows_pad, A->max_col, k, epi);
+        else if (cs)
+          ell_warp_kernel<V, XT, Epi, true, 1><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                    A->rows_pad, A->max_col, k, epi);
+        else if (R == 4)
+          ell_warp_kernel<V, XT, Epi, false, 4><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                     A->rows_pad, A->max_col, k, epi);
+        else if (R == 2)
+          ell_warp_kernel<V, XT, Epi, false, 2><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                     A->rows_pad, A->max_col, k, epi);
         else
-          ell_warp_kernel<V, XT, Epi, false><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows, A->rows_pad,
-                                                                  A->max_col, xkeep_of<XT>(A), epi);
+          ell_warp_kernel<V, XT, Epi, false, 1><<<grid, 256, 0, s>>>(A->idx0, vals, x, A->f_col, A->rows,
+                                                                     A->rows_pad, A->max_col, k, epi);
       } else {
         // four consecutive rows per thread
         const int threads = (A->rows + 3) / 4;

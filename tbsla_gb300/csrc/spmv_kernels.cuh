@@ -370,42 +370,44 @@ template <> __device__ __forceinline__ __nv_bfloat16 ld_ell<false, __nv_bfloat16
   return __ushort_as_bfloat16(u);
 }
 
-template <typename V, typename XT, typename Epi, bool CS>
+template <typename V, typename XT, typename Epi, bool CS, int R = 4>
 __global__ void __launch_bounds__(256) ell_warp_kernel(const int *__restrict__ cols,
                                                        const V *__restrict__ vals,
                                                        const XT *__restrict__ x, int f_col, int rows,
                                                        int rows_pad, int max_col, XKeep x_keep, Epi epi) {
   using Acc = typename Epi::Acc;
   if (!epi.active()) return;
-  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * 128;
+  const int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32 * (32 * R);
   const int lane = threadIdx.x & 31;
   typename Epi::State es{};
   if (base < rows) {
     const uint64_t keep = policy_keep(x_keep, x);
     const int r0 = (int)base + lane;
-    bool in[4];
+    bool in[R];
     #pragma unroll
-    for (int q = 0; q < 4; ++q) in[q] = r0 + 32 * q < rows;
-    Acc a[4] = {0, 0, 0, 0};
+    for (int q = 0; q < R; ++q) in[q] = r0 + 32 * q < rows;
+    Acc a[R];
+    #pragma unroll
+    for (int q = 0; q < R; ++q) a[q] = 0;
     #pragma unroll 4
     for (int s = 0; s < max_col; ++s) {
       const size_t off = (size_t)s * rows_pad + r0;
-      int c[4];
-      V v[4];
+      int c[R];
+      V v[R];
       #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < R; ++q) {
         c[q] = in[q] ? ld_ell<CS>(cols + off + 32 * q) : 0;
         v[q] = in[q] ? ld_ell<CS>(vals + off + 32 * q) : V(0);
       }
       #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < R; ++q) {
         int idx = c[q] - f_col;
         if (idx < 0) idx = 0;
         if (in[q]) a[q] = fma_acc(to_acc(v[q], Acc()), to_acc(ld_keep(x + idx, keep), Acc()), a[q]);
       }
     }
     #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < R; ++q)
       if (in[q]) epi.emit(r0 + 32 * q, a[q], es);
   }
   epi.block_done(es, blockIdx.x);

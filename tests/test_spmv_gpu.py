@@ -208,10 +208,10 @@ def test_csr_kernel_variants(gpu, orc, variant):
 
 
 def test_ell_kernel_variants(gpu, orc):
-    """ELL warp tiles (variant 0: lane l of a warp sums rows l, l+32, l+64,
-    l+96 of a 128-row tile) and four consecutive rows per thread (variant 1)
-    sum each row slot by slot: results are bit-identical and within the FP64
-    bound of the oracle.  Row counts that fill no tile, one row, padding
+    """ELL warp tiles (variant 0: lane l of a warp sums rows l, l+32, ... of
+    a tile of 32, 64 or 128 rows) and four consecutive rows per thread
+    (variant 1) sum each row slot by slot: results are bit-identical and
+    within the FP64 bound of the oracle.  Row counts that fill no tile, one row, padding
     slots, columns below f_col (read as x[0]), reduced-precision stores."""
     rng = np.random.default_rng(12)
     for (nr, nc, w, f_col) in [(1, 7, 3, 0), (127, 300, 5, 0), (129, 129, 16, 0), (5000, 4000, 9, 2),
@@ -242,6 +242,12 @@ def test_ell_kernel_variants(gpu, orc):
             got[variant] = outs
         for a, b in zip(got[0], got[1]):
             assert np.array_equal(a, b)
+        # warp tiles with 1, 2 or 4 rows per thread (TBSLA_TUNE_SELL_ROWS):
+        # the same bits
+        m.set_variant(0)
+        for rows_per_thread in (1, 4, 2):
+            m.tune(gpu.TUNE_SELL_ROWS, rows_per_thread)
+            assert np.array_equal(m.spmv_host(x), got[0][0]), rows_per_thread
 
 
 def test_csr_tiny_rows_kernel(gpu, orc):
