@@ -915,6 +915,23 @@ def run_gb300(args, world, rank, local, pg):
     for _ in range(args.steps):
         capi.check(L.tbsla_spmv_host(A.h, hx, n, hy, n, 0))
     e2e_s = max_over_ranks(pg, (time.perf_counter() - t0) / args.steps)
+    # the host link's rates for the same vectors (copy engine, pinned host
+    # memory): x in and y out can take no less than n*8/h2d + n*8/d2h
+    hx_t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    d_t = torch.empty(n, dtype=torch.float64, device="cuda")
+    link = {}
+    for name, (dst, src) in (("h2d", (d_t, hx_t)), ("d2h", (hx_t, d_t))):
+        for _ in range(2):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        link[name] = e0.elapsed_time(e1) / 5
+    del hx_t, d_t
     L.tbsla_host_free(hx)
     L.tbsla_host_free(hy)
     capi.check(L.tbsla_set_l2_persisting(sa0.value))
@@ -953,7 +970,10 @@ def run_gb300(args, world, rank, local, pg):
         "cpu_baseline": {"value": round(cpu_gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                          "sample": "full matrix, median of 5 products (oracle CSR loop, OpenMP over rows)"},
         "e2e": {"value": round(algo / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": n * 8,
-                "d2h_bytes_per_step": n * 8, "ms_per_step": round(e2e_s * 1e3, 3)},
+                "d2h_bytes_per_step": n * 8, "ms_per_step": round(e2e_s * 1e3, 3),
+                "host_link_GB_s": {k: round(n * 8 / (v * 1e-3) / 1e9, 1) for k, v in link.items()},
+                "transfer_floor_ms": round(link["h2d"] + link["d2h"], 3),
+                "of_transfer_floor": round((link["h2d"] + link["d2h"]) / (e2e_s * 1e3), 3)},
         "gpu_launches": kernels * args.steps,
         "clocks": clocks,
         "setup_s": round(setup_s, 2),
