@@ -328,9 +328,14 @@ tbsla_status_t tbsla_a_axpx_host(tbsla_matrix_t *A, const double *x, int64_t nx,
  * first call on a device looks the array up (cudaGetSymbolAddress) and
  * should come before any stream capture on that device.  All calls share the
  * array: calls that overlap on the GPU race and must be ordered by the
- * caller. */
+ * caller.  The inputs are checked on the device, without waiting: rows that
+ * decrease or leave [0, n_row), or columns outside [0, n_col), stop the
+ * product before it reads x, and y is filled with NaN. */
 tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t nnz, const int *d_row, const int *d_col,
                                       const double *d_values, const double *d_x, double *d_y, void *stream);
+/* Waits for `stream` and reports the input check of the device's last
+ * tbsla_coo_spmv_noalloc call: *bad = 1 when it failed (y is NaN), else 0. */
+tbsla_status_t tbsla_coo_spmv_noalloc_status(int *bad, void *stream);
 
 /* -------------------------------------------------------------- batches */
 /* Many CSR handles multiplied together: y_m = A_m x_m for every member in

@@ -22,6 +22,13 @@
 // the call), but two calls that overlap on the GPU -- on different streams,
 // or from different host threads -- race on the array and must be ordered by
 // the caller.
+//
+// Checked input: a first kernel verifies that the rows are nondecreasing and
+// inside [0, n_row) and the columns inside [0, n_col), into a flag in the
+// same array.  The product's kernels read the flag before touching x or y
+// and stand down when it is set; y is then filled with NaN, and
+// tbsla_coo_spmv_noalloc_status reports the failure to a caller that
+// synchronises.  No call waits on the GPU.
 #include <mutex>
 
 #include "driver.cuh"
@@ -38,7 +45,8 @@ constexpr size_t kOffHeadRow = 0;
 constexpr size_t kOffEmitted = kOffHeadRow + (size_t)kNoAllocMaxTiles * sizeof(int);
 constexpr size_t kOffHeadVal = (kOffEmitted + (size_t)kNoAllocMaxTiles + 255) / 256 * 256;
 constexpr size_t kOffTailVal = kOffHeadVal + (size_t)kNoAllocMaxTiles * sizeof(double);
-constexpr size_t kNoAllocBytes = kOffTailVal + (size_t)kNoAllocMaxTiles * sizeof(double);  // 344,064 B
+constexpr size_t kOffCheck = kOffTailVal + (size_t)kNoAllocMaxTiles * sizeof(double);
+constexpr size_t kNoAllocBytes = kOffCheck + 256;  // 344,320 B
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -71,9 +79,43 @@ static tbsla_status_t noalloc_scratch(unsigned char **out) {
   return TBSLA_OK;
 }
 
+// *bad = 1 when a row decreases or leaves [0, n_row), or a column leaves
+// [0, n_col) (the flag is cleared before the launch)
+__global__ void noalloc_check_kernel(int64_t nnz, const int *__restrict__ row, const int *__restrict__ col,
+                                     int n_row, int n_col, int *bad) {
+  bool ok = true;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = row[i], c = col[i];
+    ok = ok && r >= 0 && r < n_row && c >= 0 && c < n_col && (i + 1 == nnz || r <= row[i + 1]);
+  }
+  if (!ok) atomicOr(bad, 1);
+}
+
+// the product's epilogue, standing down when the input check failed
+struct CheckedStoreEpi : StoreEpi<double, double> {
+  const int *bad;
+  __device__ __forceinline__ bool active() const { return *(volatile const int *)bad == 0; }
+};
+
+// y = NaN when the input check failed
+__global__ void noalloc_poison_kernel(double *y, int n, const int *bad) {
+  if (*(volatile const int *)bad == 0) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = __longlong_as_double(0x7ff8000000000000ll);
+}
+
 }  // namespace tbsla
 
 using namespace tbsla;
+
+extern "C" tbsla_status_t tbsla_coo_spmv_noalloc_status(int *bad, void *stream) {
+  TB_CHECK(bad, "bad is NULL");
+  unsigned char *scratch = nullptr;
+  TB_TRY(noalloc_scratch(&scratch));
+  TB_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  TB_CUDA(cudaMemcpy(bad, scratch + kOffCheck, sizeof(int), cudaMemcpyDeviceToHost));
+  return TBSLA_OK;
+}
 
 extern "C" tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t nnz, const int *d_row,
                                                  const int *d_col, const double *d_values, const double *d_x,
@@ -88,16 +130,24 @@ extern "C" tbsla_status_t tbsla_coo_spmv_noalloc(int n_row, int n_col, int64_t n
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
   unsigned char *scratch = nullptr;
   TB_TRY(noalloc_scratch(&scratch));
+  int *bad = reinterpret_cast<int *>(scratch + kOffCheck);
+  TB_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
   if (n_row > 0) TB_CUDA(cudaMemsetAsync(d_y, 0, (size_t)n_row * sizeof(double), s));
   if (nnz == 0) return TBSLA_OK;
+  noalloc_check_kernel<<<152 * 8, 256, 0, s>>>(nnz, d_row, d_col, n_row, n_col, bad);
   const int tiles = (int)((nnz + kMergeTile - 1) / kMergeTile);
   const Carry<double> carry{reinterpret_cast<int *>(scratch + kOffHeadRow),
                             reinterpret_cast<double *>(scratch + kOffHeadVal),
                             reinterpret_cast<double *>(scratch + kOffTailVal), scratch + kOffEmitted};
-  StoreEpi<double, double> epi{d_y, n_row, 0};
-  coo_merge_kernel<kMergeThreads, kMergeItems, double, double, StoreEpi<double, double>>
+  CheckedStoreEpi epi;
+  epi.y = d_y;
+  epi.n_out = n_row;
+  epi.shift = 0;
+  epi.bad = bad;
+  coo_merge_kernel<kMergeThreads, kMergeItems, double, double, CheckedStoreEpi>
       <<<tiles, kMergeThreads, 0, s>>>(d_row, d_col, d_values, d_x, 0, nnz, carry, epi);
-  merge_fixup_kernel<StoreEpi<double, double>><<<(tiles + 255) / 256, 256, 0, s>>>(tiles, carry, epi);
+  merge_fixup_kernel<CheckedStoreEpi><<<(tiles + 255) / 256, 256, 0, s>>>(tiles, carry, epi);
+  if (n_row > 0) noalloc_poison_kernel<<<152 * 4, 256, 0, s>>>(d_y, n_row, bad);
   TB_CUDA(cudaGetLastError());
   return TBSLA_OK;
 }

@@ -129,3 +129,44 @@ def test_no_alloc_rejects_oversized_input(gpu):
     status = f(10, 10, too_many, None, None, None, None, None, None)
     assert status == 1  # TBSLA_ERR_INVALID_ARG, nothing launched
     assert b"exceeds" in gpu.lib().tbsla_last_error()
+
+
+def test_no_alloc_checks_its_input(gpu):
+    """Rows that decrease or leave [0, n_row), and columns outside [0, n_col),
+    are caught by the call's input check: the product stands down before
+    reading x, y is all NaN and tbsla_coo_spmv_noalloc_status reports 1; a
+    valid call afterwards reports 0.  (x is allocated 64 entries longer than
+    n_col, so that the out-of-range column stays inside the buffer.)"""
+    f = _noalloc(gpu)
+    L = gpu.lib()
+    L.tbsla_coo_spmv_noalloc_status.argtypes = [C.POINTER(C.c_int), C.c_void_p]
+
+    def status():
+        bad = C.c_int(-1)
+        gpu.check(L.tbsla_coo_spmv_noalloc_status(C.byref(bad), None))
+        return bad.value
+
+    nr, nc = 5000, 4000
+    row, col, val = _banded_coo(nr, nc, 5, 11)
+    x = np.random.default_rng(12).uniform(-1, 1, nc + 64)
+    dx = _Dev(gpu, x)
+    bad_rows = row.copy()
+    bad_rows[1000], bad_rows[1001] = bad_rows[1001] + 1, bad_rows[1000]  # a decrease, rows in range
+    bad_cols = col.copy()
+    bad_cols[777] = nc  # one past the last column
+    high_row = row.copy()
+    high_row[-1] = nr  # one past the last row (the last row stays nondecreasing)
+    for (r, c) in ((bad_rows, col), (row, bad_cols), (high_row, col)):
+        drow, dcol, dval = _Dev(gpu, r), _Dev(gpu, c), _Dev(gpu, val)
+        dy = _Dev(gpu, np.zeros(nr))
+        gpu.check(f(nr, nc, r.size, drow.p, dcol.p, dval.p, dx.p, dy.p, None))
+        assert status() == 1
+        assert np.isnan(dy.get()).all()
+    drow, dcol, dval = _Dev(gpu, row), _Dev(gpu, col), _Dev(gpu, val)
+    dy = _Dev(gpu, np.zeros(nr))
+    gpu.check(f(nr, nc, row.size, drow.p, dcol.p, dval.p, dx.p, dy.p, None))
+    assert status() == 0
+    y = dy.get()
+    ref = np.zeros(nr)
+    np.add.at(ref, row, val * x[col])
+    assert np.allclose(y, ref, rtol=1e-12, atol=1e-12)
