@@ -775,10 +775,10 @@ def differentiation_bench(capi, scale=22):
         "finite_differences": fd}
     G.close()
     torch.cuda.empty_cache()
-    # backward of y = A x, cqmat 2^24, FP32; the transposed product with the
-    # format sweep's L2 settings (64 MiB set-aside holding all of the FP32
-    # vector it gathers; restored after), the values gradient (no evict-last
-    # loads: it loses 7 % to the smaller normal L2) with the context's
+    # backward of y = A x, cqmat 2^24, FP32; the values gradient and the
+    # transposed product with the format sweep's L2 settings (64 MiB set-aside
+    # holding all of the FP32 vector they gather; restored after), the
+    # gradient also with the context's set-aside
     N = N_HEADLINE
     L = capi.lib()
     sa0, sa_max = C.c_size_t(), C.c_size_t()
@@ -801,14 +801,21 @@ def differentiation_bench(capi, scale=22):
         A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
         A.spmv_transpose_ex(capi.F32, capi.F32, gy.data_ptr(), capi.F32, gx.data_ptr(), s)
     reps = 10
-    e0, e1 = _events()
-    e0.record()
-    for _ in range(reps):
-        A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
-    e1.record()
-    torch.cuda.synchronize()
-    gv_ms = e0.elapsed_time(e1) / reps
+
+    def grad_ms():
+        for _ in range(3):
+            A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
+        e0, e1 = _events()
+        e0.record()
+        for _ in range(reps):
+            A.grad_values(capi.F32, gy.data_ptr(), xv.data_ptr(), 1.0, gval.data_ptr(), s)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    gv_ctx_ms = grad_ms()  # the context's set-aside
     capi.check(L.tbsla_set_l2_persisting(min(L2_PERSIST_BYTES, sa_max.value)))
+    gv_ms = grad_ms()  # 64 MiB set-aside, the gathered FP32 vector evict-last
+    e0, e1 = _events()
     for _ in range(3):
         A.spmv_transpose_ex(capi.F32, capi.F32, gy.data_ptr(), capi.F32, gx.data_ptr(), s)
     e0.record()
@@ -821,9 +828,11 @@ def differentiation_bench(capi, scale=22):
     tr_bytes = st * 8 + (N + 1) * 4 + 2 * N * 4
     out["spmv_backward_cqmat_2^24_f32"] = {
         "stored": st, "grad_values_ms": round(gv_ms, 4), "grad_values_GB_s": round(gv_bytes / gv_ms / 1e6, 1),
+        "grad_values_context_setaside_ms": round(gv_ctx_ms, 4),
         "transpose_product_ms": round(tr_ms, 4), "transpose_product_GB_s": round(tr_bytes / tr_ms / 1e6, 1),
         "transpose_build_s": round(build_s, 2),
-        "l2": "transposed product: 64 MiB persisting set-aside, all of the FP32 vector evict-last"}
+        "l2": "values gradient and transposed product: 64 MiB persisting set-aside, all of the gathered FP32 "
+              "vector evict-last"}
     A.close()
     capi.check(L.tbsla_set_l2_persisting(sa0.value))
     torch.cuda.empty_cache()

@@ -34,7 +34,8 @@ __global__ void __launch_bounds__(256) grad_short_kernel(const int *__restrict__
   }
 }
 
-// All rows short and consecutive: a warp takes 32 rows [r0, r0 + 32) and
+// All rows short and consecutive (b, the gathered vector, read with the
+// handle's L2 policy for x, TBSLA_TUNE_X_L2_KEEP): a warp takes 32 rows [r0, r0 + 32) and
 // strides its lanes over the segment's entries, so index loads and gradient
 // stores are coalesced; a lane finds the row of its entry by a binary search
 // over the 32 row starts held one per lane (shuffles).  Four strides of the
@@ -45,9 +46,10 @@ template <typename T>
 __global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *__restrict__ rowptr,
                                                           const int *__restrict__ colidx, int f_col,
                                                           const T *__restrict__ a, const T *__restrict__ b,
-                                                          T scale, T *__restrict__ out) {
+                                                          T scale, T *__restrict__ out, XKeep b_keep) {
   constexpr int U = 4;
   const int lane = threadIdx.x & 31;
+  const uint64_t keep = policy_keep(b_keep, b);
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * 32 < rows; w += nwarps) {
     const int r0 = (int)(w * 32);
@@ -67,7 +69,7 @@ __global__ void __launch_bounds__(256) grad_segment_kernel(int rows, const int *
       #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int e = e0 + 32 * u + lane;
-        bv[u] = e < end ? __ldg(b + (col[u] - f_col)) : T(0);
+        bv[u] = e < end ? ld_keep(b + (col[u] - f_col), keep) : T(0);
       }
       #pragma unroll
       for (int u = 0; u < U; ++u) {
@@ -116,7 +118,7 @@ tbsla_status_t grad_values(const tbsla_matrix *A, const T *a, const T *b, T scal
   if (A->short_rows == nullptr && A->n_short == A->rows) {  // every row short, in order
     const int warps = (A->rows + 31) / 32;
     grad_segment_kernel<T><<<(int)std::min<int64_t>(((int64_t)warps + 7) / 8, 152 * 64), 256, 0, s>>>(
-        A->rows, A->idx0, A->idx1, A->f_col, a, b, scale, out);
+        A->rows, A->idx0, A->idx1, A->f_col, a, b, scale, out, xkeep_of<T>(A));
     TB_CUDA(cudaGetLastError());
     return TBSLA_OK;
   }
