@@ -299,7 +299,10 @@ tbsla_status_t tbsla_matrix_device_status(const tbsla_matrix_t *A, int *status);
  * X has x_extent rows, Y n_row rows).  FP64 vectors for the F64 store, FP32
  * for F32 and BF16.  Vectors go in panels of up to 32, a group of lanes per
  * row with lane c on vector c: one gather brings a row of X for the panel,
- * and the matrix is streamed once per panel.  Column c equals the one-vector
+ * and the matrix is streamed once per panel.  FP32 panels of 4, 8 or 12
+ * vectors of a handle with the ELL-layout copy (TBSLA_TUNE_SHORT_ROWS 3) are
+ * multiplied over the copy instead, one thread per row, when ldx, ldy and
+ * the blocks' addresses allow 16-byte loads.  Column c equals the one-vector
  * product of vector c summed in stored order (bit for bit for rows of at most
  * 32 entries with TBSLA_TUNE_SHORT_ROWS = 0).  No reference counterpart (the
  * reference multiplies one vector at a time). */

@@ -67,11 +67,83 @@ __global__ void __launch_bounds__(256) csr_spmm_kernel(int rows, const int *__re
   }
 }
 
+// FP32 panels of handles with the ELL-layout copy (csr_sell_kernel's
+// arrays): one thread per row, all 4 KW vectors of the panel; for each slot
+// the warp's 32 rows load their indices and values as one 128-byte run each,
+// and the gathered X rows of neighbouring rows' band entries are neighbouring
+// rows of X.  Each vector's sum is one FMA per entry in stored order, as in
+// csr_spmm_kernel: the same bits.
+template <int KW>
+__global__ void __launch_bounds__(256) sell_spmm_kernel(const int *__restrict__ cols, const float *__restrict__ vals,
+                                                       int64_t stride, int width, int rows,
+                                                       const float *__restrict__ X, int64_t ldx, int f_col,
+                                                       float *__restrict__ Y, int64_t ldy, int row_shift, int n_out) {
+  constexpr int U = KW <= 2 ? 4 : 2;  // slots in flight
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  float acc[4 * KW];
+  #pragma unroll
+  for (int q = 0; q < 4 * KW; ++q) acc[q] = 0.f;
+  for (int j0 = 0; j0 < width; j0 += U) {
+    int c[U];
+    float v[U];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool in = j0 + u < width;
+      c[u] = in ? ld_ell<false>(cols + (size_t)(j0 + u) * stride + r) : -1;
+      v[u] = in ? ld_ell<false>(vals + (size_t)(j0 + u) * stride + r) : 0.f;
+    }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (c[u] < 0) continue;  // padding (past the row's end)
+      const float4 *xp = reinterpret_cast<const float4 *>(X + (int64_t)(c[u] - f_col) * ldx);
+      #pragma unroll
+      for (int q = 0; q < KW; ++q) {
+        const float4 x4 = __ldg(xp + q);
+        acc[4 * q + 0] = fmaf(v[u], x4.x, acc[4 * q + 0]);
+        acc[4 * q + 1] = fmaf(v[u], x4.y, acc[4 * q + 1]);
+        acc[4 * q + 2] = fmaf(v[u], x4.z, acc[4 * q + 2]);
+        acc[4 * q + 3] = fmaf(v[u], x4.w, acc[4 * q + 3]);
+      }
+    }
+  }
+  const int out = r + row_shift;
+  if (out >= 0 && out < n_out) {
+    float4 *yp = reinterpret_cast<float4 *>(Y + (int64_t)out * ldy);
+    #pragma unroll
+    for (int q = 0; q < KW; ++q) yp[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+  }
+}
+
 template <typename V, typename T>
 tbsla_status_t spmm_panel(const tbsla_matrix *A, const int *rowptr, const V *vals, const T *X, int64_t ldx, T *Y,
                           int64_t ldy, int width, int row_shift, cudaStream_t s) {
   const int rows = A->rows;
   if (rows <= 0) return TBSLA_OK;
+  if constexpr (std::is_same<V, float>::value && std::is_same<T, float>::value) {
+    // the ELL-layout copy (default short-row mode, or 3), when the panel is
+    // whole float4 runs on both sides and at most 12 wide (cqmat 2^22, ms
+    // copy / CSR arrays: k = 4 0.146 / 0.339, 8 0.235 / 0.377, 12 0.325 /
+    // 0.445, 16 0.598 / 0.458, 32 1.912 / 0.669: a thread's 4 k
+    // accumulators and gathers crowd out the loads in flight above 12)
+    if (A->sell_width && A->sell_vals[1] && vals == A->values[1] && (A->short_mode == -1 || A->short_mode == 3) &&
+        width % 4 == 0 && width <= 12 && ldx % 4 == 0 && ldy % 4 == 0 &&
+        (reinterpret_cast<uintptr_t>(X) & 15) == 0 && (reinterpret_cast<uintptr_t>(Y) & 15) == 0) {
+      const float *sv = static_cast<const float *>(A->sell_vals[1]);
+      const int grid = (rows + 255) / 256;
+#define TB_SELL_SPMM(KW_)                                                                                          \
+  sell_spmm_kernel<KW_><<<grid, 256, 0, s>>>(A->sell_cols, sv, A->sell_stride, A->sell_width, rows, X, ldx, A->f_col, \
+                                             Y, ldy, row_shift, A->n_row)
+      switch (width / 4) {
+      case 1: TB_SELL_SPMM(1); break;
+      case 2: TB_SELL_SPMM(2); break;
+      default: TB_SELL_SPMM(3); break;
+      }
+#undef TB_SELL_SPMM
+      TB_CUDA(cudaGetLastError());
+      return TBSLA_OK;
+    }
+  }
   // 16-byte loads of X rows when the panel is whole 16-byte chunks, aligned
   constexpr int VW16 = 16 / (int)sizeof(T);
   const bool vec = width % VW16 == 0 && (ldx * (int64_t)sizeof(T)) % 16 == 0 &&

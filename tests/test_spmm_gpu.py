@@ -75,3 +75,32 @@ def test_spmm_coo_and_partial_rows(gpu, orc):
     assert np.all(Y[100:] == 0)
     for c in range(4):
         assert np.array_equal(Y[:, c], m.spmv_host(np.ascontiguousarray(X[:, c])))
+
+
+def test_spmm_f32_over_ell_layout_copy(gpu, orc):
+    """FP32 panels of a handle with the ELL-layout copy (every row short and
+    even, at least 2^16 rows) take sell_spmm_kernel when the panel and the
+    leading dimensions are whole float4 runs: each vector summed in stored
+    order, so Y equals the CSR-array kernel (TBSLA_TUNE_SHORT_ROWS = 0) bit for
+    bit, and the oracle within the FP32 bound; panels of 4, 8 or 12 vectors
+    take it, other widths the CSR arrays."""
+    rng = np.random.default_rng(53)
+    nr = nc = 70000
+    lens = np.full(nr, 12)
+    lens[rng.choice(nr, 500, replace=False)] = 10
+    rp, ci, va = random_csr(rng, nr, nc, lens)
+    m = gpu.DeviceMatrix.csr(nr, nc, rp, ci, va, stores=gpu.STORE_F64 | gpu.STORE_F32)
+    assert m.info().slices > 0
+    o = orc.from_arrays("CSR", nr, nc, va, rp, ci)
+    so = orc.from_arrays("CSR", nr, nc, np.abs(va), rp, ci)
+    for k, ldx in ((4, 4), (8, 8), (32, 32), (40, 44), (12, 16), (6, 8), (8, 9)):
+        X = rng.uniform(-1, 1, (nc, k)).astype(np.float32)
+        m.tune(gpu.TUNE_SHORT_ROWS, -1)
+        Y = _run(gpu, m, gpu.F32, X, k, ldx, nr, torch.float32)
+        m.tune(gpu.TUNE_SHORT_ROWS, 0)
+        Y0 = _run(gpu, m, gpu.F32, X, k, ldx, nr, torch.float32)
+        assert np.array_equal(Y, Y0), (k, ldx)
+        for c in (0, k - 1):
+            xc = X[:, c].astype(np.float64)
+            assert_close(Y[:, c], o.spmv(xc), so.spmv(np.abs(xc)), 2e-6, f"sliced spmm k={k} c={c}")
+    m.tune(gpu.TUNE_SHORT_ROWS, -1)
