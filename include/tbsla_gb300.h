@@ -373,7 +373,8 @@ typedef struct {
   float best_ms;    /* time of the kept one                     */
   int choice;       /* spmv: 0 direct, 1 row blocks, 2 staged short rows,
                        3 two lanes per short row, 4 warp tiles of tiny
-                       rows (every row at most 4 entries);
+                       rows (every row at most 4 entries), 5 the
+                       ELL-layout copy (TBSLA_TUNE_SHORT_ROWS 3);
                        batch: blocks per SM; ppr: tile */
   double value;     /* spmv: x L2-keep fraction; otherwise = choice */
 } tbsla_autotune_result_t;

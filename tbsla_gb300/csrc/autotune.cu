@@ -69,22 +69,27 @@ tbsla_status_t tbsla_autotune_spmv(tbsla_matrix_t *A, tbsla_dtype_t store, tbsla
   // kernels: 0 direct, 1 row blocks (CSR), 2 direct with the staged
   // short-row kernel (every row at most 32 entries), 3 direct with two lanes
   // per short row, 4 direct with warp tiles of tiny rows (every row at most
-  // kTinyRow entries, in order: the default rule, TBSLA_TUNE_SHORT_ROWS -1)
+  // kTinyRow entries, in order: the default rule, TBSLA_TUNE_SHORT_ROWS -1),
+  // 5 the ELL-layout copy (TBSLA_TUNE_SHORT_ROWS 3; F64 / F32 stores of
+  // handles that keep one)
   const bool csr = A->format == TBSLA_FMT_CSR;
   const bool tiny = A->n_short > 0 && A->short_rows == nullptr && A->short_max <= kTinyRow;
-  auto mode_of = [](int v) { return v == 2 ? 1 : v == 3 ? 2 : v == 4 ? -1 : 0; };
+  const bool sliced = A->sell_width > 0 && store != TBSLA_BF16 && A->sell_vals[store == TBSLA_F64 ? 0 : 1];
+  auto mode_of = [](int v) { return v == 2 ? 1 : v == 3 ? 2 : v == 4 ? -1 : v == 5 ? 3 : 0; };
   float best = 1e30f;
   int best_v = A->csr_variant == 1 ? 1 : A->short_mode == 1 ? 2 : A->short_mode == 2 ? 3
+               : (A->short_mode < 0 || A->short_mode == 3) && sliced ? 5
                : (A->short_mode < 0 && tiny) ? 4 : 0;
   const int mode_in = A->short_mode;
   float best_k = A->x_keep;
   tbsla_status_t st = TBSLA_OK;
   int tried = 0;
-  for (int v = 0; v < 5 && st == TBSLA_OK; ++v) {
+  for (int v = 0; v < 6 && st == TBSLA_OK; ++v) {
     if (v == 1 && !csr) continue;
     if (v == 2 && A->stage_cap == 0) continue;
     if (v == 3 && A->n_short == 0) continue;
     if (v == 4 && !tiny) continue;
+    if (v == 5 && !sliced) continue;
     for (float k : keeps) {
       if (csr) A->csr_variant = v == 1 ? 1 : 0;
       A->short_mode = mode_of(v);

@@ -294,6 +294,22 @@ def test_autotune_tries_tiny_rows(gpu):
     assert np.array_equal(m.spmv_host(x), before)
 
 
+def test_autotune_tries_sliced_copy(gpu):
+    """On a handle with the ELL-layout copy the SpMV autotuner also times the
+    copy (choice 5, TBSLA_TUNE_SHORT_ROWS 3) with four x-keep fractions, next
+    to one thread per row, row blocks, staged tiles and two lanes per row;
+    integer-valued products stay exact whatever it keeps."""
+    n = 70000
+    m = gpu.DeviceMatrix.from_generated(gpu.generate("CSR", "cqmat", n, n, 12, 0.1, 3))
+    assert m.info().slices > 0
+    x = np.arange(n, dtype=np.float64)
+    before = m.spmv_host(x)
+    r = m.autotune_spmv(gpu.F64)
+    # 4 keeps x (direct, staged, pairs, copy) + 1 row-block run
+    assert r.candidates == 17 and r.choice in (0, 1, 2, 3, 5)
+    assert np.array_equal(m.spmv_host(x), before)
+
+
 def test_coo_unsorted_duplicates_and_shift(gpu, orc):
     rng = np.random.default_rng(4)
     for (nr, nc, nnz) in [(50, 40, 700), (1000, 800, 30000), (7, 7, 0), (1, 1, 5), (40000, 3, 90000)]:
