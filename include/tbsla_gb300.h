@@ -198,6 +198,10 @@ tbsla_status_t tbsla_matrix_set_variant(tbsla_matrix_t *A, int variant);
  *                         3 % from 7e4 to 1.6e7 rows (cqmat 2^24 FP64: CSR
  *                         copy 0.625 ms, 4 rows 0.646 ms; ELL 0.629 against
  *                         0.649 ms).  Results do not depend on it.
+ *   TBSLA_TUNE_DROP_SLICED_COPY  1: frees the handle's ELL-layout copy (the
+ *                         copy doubles the device memory of the entries);
+ *                         products then read the CSR arrays.  Waits for the
+ *                         device; the copy is not rebuilt.
  *   TBSLA_TUNE_PR_RELABEL PageRank on a copy of a CSR graph relabelled in
  *                         decreasing out-degree order (built on first use,
  *                         kept with the handle): 1 on, 0 off, -1 (default)
@@ -219,7 +223,8 @@ typedef enum {
   TBSLA_TUNE_X_L2_RANGE = 2,
   TBSLA_TUNE_SHORT_ROWS = 3,
   TBSLA_TUNE_TC_SPLIT = 4,
-  TBSLA_TUNE_SELL_ROWS = 5
+  TBSLA_TUNE_SELL_ROWS = 5,
+  TBSLA_TUNE_DROP_SLICED_COPY = 6
 } tbsla_tune_knob_t;
 tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value);
 tbsla_status_t tbsla_matrix_info(const tbsla_matrix_t *A, tbsla_matrix_info_t *info);

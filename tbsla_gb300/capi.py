@@ -22,6 +22,7 @@ F64, F32, BF16 = 0, 1, 2
 STORE_F64, STORE_F32, STORE_BF16 = 1, 2, 4
 PR_REFERENCE, PR_DANGLING, PR_TELEPORT = 0, 1, 2
 TUNE_X_L2_KEEP, TUNE_PR_RELABEL, TUNE_X_L2_RANGE, TUNE_SHORT_ROWS, TUNE_TC_SPLIT, TUNE_SELL_ROWS = 0, 1, 2, 3, 4, 5
+TUNE_DROP_SLICED_COPY = 6
 GEN = {"cqmat": 0, "cdiag": 1, "cqmat_stochastic": 2, "cqmat_baseline": 3}
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")

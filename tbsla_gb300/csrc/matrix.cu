@@ -843,6 +843,25 @@ tbsla_status_t tbsla_matrix_tune(tbsla_matrix_t *A, int knob, double value) {
              "rows per thread %g not 0, 1, 2 or 4", value);
     A->sell_rows = (int)value;
     return TBSLA_OK;
+  case TBSLA_TUNE_DROP_SLICED_COPY:
+    TB_CHECK(value == 1.0, "drop the sliced copy: value %g not 1", value);
+    if (A->sell_width) {
+      TB_CUDA(cudaSetDevice(A->device));
+      TB_CUDA(cudaDeviceSynchronize());  // no product may still read it
+      const int64_t slots = A->sell_stride * A->sell_width;
+      const size_t esz[3] = {4, 8, 4};  // columns, F64, F32 values
+      void *bufs[3] = {A->sell_cols, A->sell_vals[0], A->sell_vals[1]};
+      for (int k = 0; k < 3; ++k)
+        if (bufs[k]) {
+          cudaFree(bufs[k]);
+          A->device_bytes -= slots * (int64_t)esz[k] + 64;
+        }
+      A->sell_cols = nullptr;
+      A->sell_vals[0] = A->sell_vals[1] = A->sell_vals[2] = nullptr;
+      A->sell_width = 0;
+      A->sell_stride = 0;
+    }
+    return TBSLA_OK;
   case TBSLA_TUNE_X_L2_RANGE:
     TB_CHECK(value == 0.0 || value == 1.0, "x L2 range mode %g not 0 or 1", value);
     A->x_keep_range = (int)value;

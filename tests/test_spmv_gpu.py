@@ -640,6 +640,11 @@ def test_csr_sliced_copy(gpu, orc):
     assert mp.info().slices > 0
     yp = mp.spmv_host(x)
     assert np.array_equal(yp[part:], np.zeros(n - part)) and np.array_equal(yp[:part], y_sliced[:part])
+    # dropped on request: the memory returns, the products read the CSR arrays
+    held = m.info().device_bytes
+    m.tune(gpu.TUNE_DROP_SLICED_COPY, 1)
+    assert m.info().slices == 0 and m.info().device_bytes < held
+    assert np.array_equal(m.spmv_host(x), y2)
     # not built: a row longer than 32 entries; padding above 1/32; short rows
     for bad in (np.r_[np.full(n - 1, 12), 40], np.r_[np.full(n // 2, 12), np.full(n - n // 2, 6)],
                 np.full(n, 3)):
