@@ -348,8 +348,10 @@ tbsla_status_t tbsla_coo_spmv_noalloc_status(int *bad, void *stream);
 /* -------------------------------------------------------------- batches */
 /* Many CSR handles multiplied together: y_m = A_m x_m for every member in
  * ONE kernel launch (a persistent grid walking row items of every member
- * with a fixed stride, so sums are deterministic).  No reference
- * counterpart (the reference multiplies one matrix per call). */
+ * with a fixed stride, so sums are deterministic; members that keep the
+ * ELL-layout copy, TBSLA_TUNE_SHORT_ROWS 3, are read from it for the F64 and
+ * F32 stores).  No reference counterpart (the reference multiplies one
+ * matrix per call). */
 typedef struct tbsla_batch tbsla_batch_t;
 /* members: count CSR handles on one device, kept alive by the caller */
 tbsla_status_t tbsla_batch_create(int count, const tbsla_matrix_t *const *members, tbsla_batch_t **out);

@@ -7,9 +7,11 @@
 // sum is fixed and the launch needs no counter to reset: it can be replayed
 // from a CUDA graph as is.  A row is summed by one thread in its stored
 // order (the thread-per-row loads of csr_direct.cuh: the single products'
-// arithmetic with TBSLA_TUNE_SHORT_ROWS = 0).  An optional device
-// mask skips members (per-instance convergence masking for iterative
-// callers).
+// arithmetic with TBSLA_TUNE_SHORT_ROWS = 0).  Members that keep the
+// ELL-layout copy (csr_sell_kernel's arrays) for the bound store are read
+// from it, two rows per thread (items of 2 * kBatchRows rows): the same sums,
+// coalesced loads.  An optional device mask skips members (per-instance
+// convergence masking for iterative callers).
 #include <algorithm>
 #include <vector>
 
@@ -23,7 +25,10 @@ struct BatchMember {
   const void *values;
   const void *x;
   void *y;
-  int f_col, rows, n_row, pad;
+  int f_col, rows, n_row, sell_width;
+  const int *sell_cols;     // the ELL-layout copy (NULL: none)
+  const void *sell_vals;    // its values for the bound store (NULL: read the CSR arrays)
+  int64_t sell_stride;
 };
 
 constexpr int kBatchRows = 256;
@@ -52,16 +57,39 @@ __global__ void __launch_bounds__(256) batch_spmv_kernel(const BatchMember *__re
       mn = members[wn.x];
       onn = !mask || mask[wn.x] != 0;
     }
-    const int r = w.y + (int)threadIdx.x;
-    if (on && r < w.z) {  // `on` is uniform across the block
+    if (on) {  // `on` is uniform across the block
       T *y = static_cast<T *>(m.y);
-      if (r >= m.rows) {
-        y[r] = T(0);
+      const T *x = static_cast<const T *>(m.x);
+      const int ra = w.y + (int)threadIdx.x, rb = ra + kBatchRows;
+      if (m.sell_vals) {
+        // rows ra and rb from the ELL-layout copy, slot by slot (padding and
+        // rows past m.rows hold column -1 or are not read)
+        const V *sv = static_cast<const V *>(m.sell_vals);
+        const bool ha = ra < w.z && ra < m.rows, hb = rb < w.z && rb < m.rows;
+        Acc sa = 0, sb = 0;
+        #pragma unroll 4
+        for (int j = 0; j < m.sell_width; ++j) {
+          const size_t off = (size_t)j * m.sell_stride;
+          const int ca = ha ? ld_ell<false>(m.sell_cols + off + ra) : -1;
+          const int cb = hb ? ld_ell<false>(m.sell_cols + off + rb) : -1;
+          const V va = ha ? ld_ell<false>(sv + off + ra) : V(0);
+          const V vb = hb ? ld_ell<false>(sv + off + rb) : V(0);
+          if (ca >= 0) sa = fma_acc(to_acc(va, Acc()), to_acc(ld_keep(x + (ca - m.f_col), keep), Acc()), sa);
+          if (cb >= 0) sb = fma_acc(to_acc(vb, Acc()), to_acc(ld_keep(x + (cb - m.f_col), keep), Acc()), sb);
+        }
+        if (ra < w.z) __stcs(y + ra, (T)sa);
+        if (rb < w.z) __stcs(y + rb, (T)sb);
       } else {
-        const int a = __ldg(m.rowptr + r), b = __ldg(m.rowptr + r + 1);
-        const Acc s = row_sum_thread<V, T, Acc>(m.colidx, static_cast<const V *>(m.values),
-                                                static_cast<const T *>(m.x), m.f_col, a, b, keep);
-        __stcs(y + r, (T)s);
+        for (int r = ra; r < w.z; r += kBatchRows) {
+          if (r >= m.rows) {
+            y[r] = T(0);
+          } else {
+            const int a = __ldg(m.rowptr + r), b = __ldg(m.rowptr + r + 1);
+            const Acc s = row_sum_thread<V, T, Acc>(m.colidx, static_cast<const V *>(m.values), x, m.f_col, a,
+                                                    b, keep);
+            __stcs(y + r, (T)s);
+          }
+        }
       }
     }
     w = wn;
@@ -128,8 +156,13 @@ tbsla_status_t tbsla_batch_create(int count, const tbsla_matrix_t *const *member
     d.f_col = A->f_col;
     d.rows = A->rows;
     d.n_row = A->n_row;
+    d.sell_width = A->sell_width;
+    d.sell_cols = A->sell_cols;
+    d.sell_stride = A->sell_stride;
     B->table.push_back(d);
-    for (int r = 0; r < A->n_row; r += kBatchRows) items.push_back(make_int4(m, r, std::min(r + kBatchRows, A->n_row), 0));
+    // members with the ELL-layout copy: items of two rows per thread
+    const int span = A->sell_width ? 2 * kBatchRows : kBatchRows;
+    for (int r = 0; r < A->n_row; r += span) items.push_back(make_int4(m, r, std::min(r + span, A->n_row), 0));
   }
   B->n_items = (int)items.size();
   cudaSetDevice(B->device);
@@ -155,6 +188,7 @@ tbsla_status_t tbsla_batch_bind(tbsla_batch_t *B, tbsla_dtype_t store, const voi
     TB_CHECK(d_y[m] || A->n_row == 0, "y of member %zu is NULL", m);
     TB_CHECK(d_x[m] || A->stored == 0, "x of member %zu is NULL", m);
     B->table[m].values = A->values[si];
+    B->table[m].sell_vals = A->sell_width && si < 2 ? A->sell_vals[si] : nullptr;
     B->table[m].x = d_x[m];
     B->table[m].y = d_y[m];
   }

@@ -23,10 +23,13 @@ def test_multi_matrix_batch_matches_single_products(gpu):
     dev = torch.device("cuda")
     members, xs, ys = [], [], []
     for m in range(12):
-        n = int(np.exp(rng.uniform(np.log(1000), np.log(60000))))
+        # two members large enough for the ELL-layout copy (read from it, two
+        # rows per thread, for the F64 and F32 stores; BF16 from the CSR arrays)
+        n = 70000 + 61000 * (m - 10) if m >= 10 else int(np.exp(rng.uniform(np.log(1000), np.log(60000))))
         c = int(rng.integers(8, 33))
         members.append(gpu.DeviceMatrix.generate("CSR", "cqmat", n, n, c, 0.1, m + 1,
                                                  stores=gpu.STORE_F64 | gpu.STORE_F32 | gpu.STORE_BF16))
+    assert members[10].info().slices > 0 and members[11].info().slices > 0
     B = gpu.Batch(members)
     for A in members:  # the batch sums each row in one thread, in stored order
         A.tune(gpu.TUNE_SHORT_ROWS, 0)
