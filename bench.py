@@ -6,18 +6,27 @@ product), in GB/s of algorithmic bytes over device time with the matrix and x
 resident in HBM.  Every section runs with 32-byte L2 fetches
 (tbsla_set_l2_fetch_granularity); the headline and the format sweep keep x
 evict-last in a 64 MiB persisting L2 set-aside (tbsla_set_l2_persisting), the
-other sections run with the context's set-aside.  A "step" is one product.  ``e2e`` is the same metric through
+other sections run with the context's set-aside (the values gradient and the
+transposed product: both).  A "step" is one product, read from the handle's
+ELL-layout copy when it keeps one (csr_sell_kernel; the CSR-array pair kernel
+is timed beside it, ``csr_pair_kernel``).  ``e2e`` is the same metric through
 the C ABI's host-vector call (tbsla_spmv_host) on pinned host vectors: x is
 copied into HBM and the product writes y into host memory over NVLink-C2C,
-both inside the timed region.
+both inside the timed region; the host link's copy rates for the same vectors,
+timed in the run, give its floor (``transfer_floor_ms``).
 
 Also reported (single-GPU runs): the format sweep of the same configuration
 (CSR/ELL/COO/SCOO FP64 SpMV and a_axpx_, CSR FP32/BF16 stores, DENSE n = 32768,
-cdiag n = 2^26) and
-PageRank on the R-MAT graph 2^24 nodes / 2^28 edge draws, (a,b,c,d) = (0.57,
-0.19, 0.19, 0.05), seed 1, damping 0.85, dangling mass redistributed, stopped at
-L1 residual 1e-10: time to tolerance in FP64 and with FP32 / BF16 stored values
-plus FP64 refinement, and each result's L1 distance to an FP64 solve at 1e-13.
+cdiag n = 2^26), the 64-vector DENSE product on the tensor cores, PageRank on
+the R-MAT graph 2^24 nodes / 2^28 edge draws, (a,b,c,d) = (0.57, 0.19, 0.19,
+0.05), seed 1, damping 0.85, dangling mass redistributed, stopped at L1
+residual 1e-10: time to tolerance in FP64 and with FP32 / BF16 stored values
+plus FP64 refinement (plain or Anderson-accelerated), each result's L1 distance
+to an FP64 solve at 1e-13 and to the oracle's, with the oracle's own times on
+the host cores; batching (64 matrices in one launch, 256 personalized PageRank
+vectors plain / accelerated / refined, k vectors through one matrix); and
+differentiation (the adjoint PageRank against finite differences on 1000
+edges of R-MAT 2^22, the backward of y = A x at 2^24).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
