@@ -521,19 +521,31 @@ tbsla_status_t csr_bins(tbsla_matrix *A, const std::vector<int> &rp) {
       const int64_t total = stride * width;
       const int64_t nnz = rp[rows];
       if (nnz >= 4ll * rows && total <= nnz + nnz / 32) {
-        const int *rpd = A->format == TBSLA_FMT_CSR ? A->idx0 : A->coo_rowptr;
-        TB_TRY(alloc_n(A, &A->sell_cols, total));
-        TB_CUDA(cudaMemset(A->sell_cols, 0xff, (size_t)total * sizeof(int)));  // padding: column -1
-        sell_scatter_kernel<int><<<grid_for(rows, 256), 256>>>(rpd, stride, rows, A->idx1, A->sell_cols);
-        const size_t esz[2] = {8, 4};
-        for (int k = 0; k < 2; ++k)  // F64 and F32 stores (BF16 products read the CSR arrays)
-          if (A->values[k]) {
-            TB_TRY(dev_alloc(A, &A->sell_vals[k], (size_t)total * esz[k]));
-            TB_CUDA(cudaMemset(A->sell_vals[k], 0, (size_t)total * esz[k]));
-          }
-        A->sell_stride = stride;
-        A->sell_width = width;
-        TB_TRY(sell_refresh(A, 0));
+        // best effort: without the device memory for it the handle keeps the
+        // CSR arrays alone (the copy doubles the entries' memory)
+        const size_t esz[3] = {4, 8, 4};  // columns, F64 and F32 values (BF16 products read the CSR arrays)
+        void **bufs[3] = {(void **)&A->sell_cols, &A->sell_vals[0], &A->sell_vals[1]};
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; ++k)
+          if (k == 0 || A->values[k - 1]) ok = dev_alloc(A, bufs[k], (size_t)total * esz[k]) == TBSLA_OK;
+        if (!ok) {
+          for (int k = 0; k < 3; ++k)
+            if (*bufs[k]) {
+              cudaFree(*bufs[k]);
+              *bufs[k] = nullptr;
+              A->device_bytes -= total * (int64_t)esz[k] + 64;
+            }
+          g_err.clear();
+        } else {
+          const int *rpd = A->format == TBSLA_FMT_CSR ? A->idx0 : A->coo_rowptr;
+          TB_CUDA(cudaMemset(A->sell_cols, 0xff, (size_t)total * sizeof(int)));  // padding: column -1
+          for (int k = 0; k < 2; ++k)
+            if (A->sell_vals[k]) TB_CUDA(cudaMemset(A->sell_vals[k], 0, (size_t)total * esz[k + 1]));
+          sell_scatter_kernel<int><<<grid_for(rows, 256), 256>>>(rpd, stride, rows, A->idx1, A->sell_cols);
+          A->sell_stride = stride;
+          A->sell_width = width;
+          TB_TRY(sell_refresh(A, 0));
+        }
       }
     }
     A->n_warp_items = (int)items.size();

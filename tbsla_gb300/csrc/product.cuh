@@ -115,11 +115,14 @@ inline int sell_rows_per_thread(const tbsla_matrix *A) {
 // mode 3; F64 and F32 stores (BF16 slots load 64 bytes per warp instruction:
 // cqmat 2^24 0.366 ms against 0.334 with one thread per row)
 template <typename V, typename Epi> inline const V *sell_vals_for(const tbsla_matrix *A, const V *vals) {
-  if (Epi::kReduces || !A->sell_width || !(A->short_mode == -1 || A->short_mode == 3)) return nullptr;
-  if (sizeof(V) < 4) return nullptr;  // BF16: the copy is not kept
-  for (int k = 0; k < 3; ++k)
-    if (A->values[k] == static_cast<const void *>(vals)) return static_cast<const V *>(A->sell_vals[k]);
-  return nullptr;
+  if constexpr (sizeof(V) < 4) {
+    return nullptr;  // BF16: the copy is not kept
+  } else {
+    if (Epi::kReduces || !A->sell_width || !(A->short_mode == -1 || A->short_mode == 3)) return nullptr;
+    for (int k = 0; k < 2; ++k)
+      if (A->values[k] == static_cast<const void *>(vals)) return static_cast<const V *>(A->sell_vals[k]);
+    return nullptr;
+  }
 }
 
 // The direct CSR launches (row bins of the handle) over rowptr / colidx:
