@@ -823,8 +823,8 @@ tbsla_status_t run_tiles_impl(const tbsla_matrix *M, const int *newid_dev, const
   }
   int rbase = 0;  // rhs_t[rbase] holds the current layout's right-hand side
   if (cudaGetLastError() != cudaSuccess) { cleanup(); return fail(TBSLA_ERR_CUDA, "batched PageRank init"); }
-  // Sweeps in rounds of K on every tile of the current layout (stopped tiles
-  // return at once).  After each round the vectors that stopped are written
+  // Sweeps in sets of K on every tile of the current layout (stopped tiles
+  // return at once).  After each set the vectors that stopped are written
   // out and dropped; when the live vectors fit in fewer tiles they are
   // repacked (compaction), so a tile never keeps sweeping for one slow
   // vector while its other lanes idle.  All tiles of a layout sweep in step:
@@ -849,7 +849,7 @@ tbsla_status_t run_tiles_impl(const tbsla_matrix *M, const int *newid_dev, const
     for (int k2 = 0; k2 < K; ++k2, ++phase, ++gk) {
       const int w = (int)(gk % 3), w1 = (int)((gk + 2) % 3), w2 = (int)((gk + 1) % 3);
       for (int t = 0; t < cur_tiles; ++t) {
-        if (!tile_live[(size_t)t]) continue;  // stopped in an earlier round
+        if (!tile_live[(size_t)t]) continue;  // stopped before this set of K sweeps
         const size_t off = (size_t)t * tstride;
         const T *xo = AA ? x[0] + off : x[(base + phase) & 1] + off;
         T *xn = AA ? g_ring[w] + off : x[(base + phase + 1) & 1] + off;
