@@ -526,7 +526,7 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def batching_bench(capi, ppr_scale=22):
+def batching_bench(capi, ppr_scale=22, ppr_vectors=256):
     """64 cqmat matrices (n log-uniform 1e3..1e6, c 8..32, q 0.1, FP32) in one
     launch vs 64 launches; 256 personalized PageRank vectors (|P| log-uniform
     1..100) on R-MAT 2^22 solved together vs one at a time."""
@@ -577,7 +577,7 @@ def batching_bench(capi, ppr_scale=22):
     # ---- 256 personalized PageRank vectors
     G = capi.DeviceMatrix.rmat_pagerank(ppr_scale, 16 << ppr_scale, seed=1, stores=capi.STORE_F64 | capi.STORE_F32)
     n = G.info().n_row
-    k = 256
+    k = ppr_vectors
     sets = [rng.integers(0, n, int(np.exp(rng.uniform(0, np.log(100))))) for _ in range(k)]
     res = {"graph": f"R-MAT scale {ppr_scale}, 2^{ppr_scale + 4} draws, seed 1", "vectors": k, "tol": 1e-10}
     ref = torch.empty(k * n, dtype=torch.float64, device=dev)
@@ -1016,6 +1016,8 @@ def main():
     ap.add_argument("--pagerank-only", action="store_true", help="only the R-MAT PageRank timings (profiling)")
     ap.add_argument("--rmat-scale", type=int, default=24, help="R-MAT graph of 2^scale vertices (profiling cases)")
     ap.add_argument("--dense-k", type=int, default=64, help="vectors of the DENSE multi-vector section")
+    ap.add_argument("--ppr-vectors", type=int, default=256, help="personalized PageRank vectors of the batching "
+                    "section (profiling cases)")
     ap.add_argument("--section", choices=["pagerank", "batching", "differentiation", "formats", "cfg1", "dense"],
                     default=None,
                     help="only one section of the full report (profiling cases)")
@@ -1028,8 +1030,8 @@ def main():
         if args.pagerank_only or args.section == "pagerank":
             print(json.dumps({"pagerank": pagerank_bench(capi, args.rmat_scale)}), flush=True)
         elif args.section == "batching":
-            print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22)}),
-                  flush=True)
+            print(json.dumps({"batching": batching_bench(capi, args.rmat_scale if args.rmat_scale != 24 else 22,
+                                                         args.ppr_vectors)}), flush=True)
         elif args.section == "dense":
             nd = 32768 if args.log2n >= 24 else 1 << (args.log2n - 9)
             print(json.dumps({"dense": dense_multi(capi, nd, args.dense_k)}), flush=True)
