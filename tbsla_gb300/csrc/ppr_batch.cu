@@ -150,6 +150,7 @@ struct PprRing {
 template <int VW>
 struct PprCols {
   double tele[VW];  // teleport term added at seed rows
+  float tele_f[VW];  // the same rounded to FP32 (FP32 tiles)
   bool stopped[VW];
   int hist[VW];  // accelerated: residuals stored before this sweep
 };
@@ -161,6 +162,7 @@ __device__ __forceinline__ void ppr_cols(PprCols<VW> &pc, int c, const ColCtl *c
     const ColCtl cc = col[c + q];
     pc.stopped[q] = cc.done != 0;
     pc.tele[q] = cc.add * inv_size[c + q];
+    pc.tele_f[q] = (float)pc.tele[q];
     pc.hist[q] = AA ? aa[c + q].hist : 0;
   }
 }
@@ -192,13 +194,18 @@ __device__ __forceinline__ void ppr_row_in(PprRowIn<T, VW, AA> &in, int row, int
 
 // New values of one finished row for a lane's VW columns:
 //   y = beta acc + [seed row] tele + rhs (a stopped column keeps its value),
-// their L1 change and dangling mass; accelerated: r = y - x into the ring
-// and its dots with the previous residuals, summed per thread in shared
-// memory (dots[(j*VW + q)*256 + thread]: registers are the sweep's limit)
-template <typename T, int VW, int NV, bool AA>
+// their L1 change (res) and dangling mass (dm, FP64: it sets the next
+// sweep's teleport term, so the fixed point); accelerated: r = y - x into
+// the ring and its dots with the previous residuals, summed per thread in
+// shared memory (dots[(j*VW + q)*256 + thread]: registers are the sweep's
+// limit).  FP32 tiles compute y, the L1 change and the dots in FP32 (the
+// per-thread sums cover a few hundred rows; the block and grid sums are
+// FP64): the FP64 pipe, two operations per clock per SM, is kept for the
+// dangling mass.
+template <typename T, int VW, bool AA>
 __device__ __forceinline__ void ppr_emit(int row, int KT, int c, const T (&acc)[VW], const PprCols<VW> &pc,
                                          const PprRowIn<T, VW, AA> &in, T *xn, double beta, bool has_rhs,
-                                         const PprRing<T> &ring, double (&part)[NV][VW], double *dots) {
+                                         const PprRing<T> &ring, T (&res)[VW], double (&dm)[VW], T *dots) {
   const size_t at = (size_t)row * KT + c;
   T y[VW];
   #pragma unroll
@@ -206,12 +213,19 @@ __device__ __forceinline__ void ppr_emit(int row, int KT, int c, const T (&acc)[
     if (pc.stopped[q]) {
       y[q] = in.old[q];
     } else {
-      double t = ((in.sd >> q) & 1u) ? pc.tele[q] : 0.0;
-      if (has_rhs) t += (double)in.rh[q];
-      y[q] = (T)((double)beta * (double)acc[q] + t);
-      part[0][q] += fabs((double)y[q] - (double)in.old[q]);
+      if constexpr (std::is_same<T, float>::value) {
+        float t = ((in.sd >> q) & 1u) ? pc.tele_f[q] : 0.f;
+        if (has_rhs) t += in.rh[q];
+        y[q] = fmaf((float)beta, acc[q], t);
+        res[q] += fabsf(y[q] - in.old[q]);
+      } else {
+        double t = ((in.sd >> q) & 1u) ? pc.tele[q] : 0.0;
+        if (has_rhs) t += (double)in.rh[q];
+        y[q] = (T)((double)beta * (double)acc[q] + t);
+        res[q] += fabs((double)y[q] - (double)in.old[q]);
+      }
     }
-    if (in.dm) part[1][q] += (double)y[q];
+    if (in.dm) dm[q] += (double)y[q];
   }
   ppr_st<T, VW>(xn + at, y);
   if constexpr (AA) {
@@ -221,12 +235,28 @@ __device__ __forceinline__ void ppr_emit(int row, int KT, int c, const T (&acc)[
     ppr_st<T, VW>(ring.r0 + at, r);
     #pragma unroll
     for (int q = 0; q < VW; ++q) {
-      double *dq = dots + (size_t)q * 256 + threadIdx.x;
-      dq[0] += (double)r[q] * (double)r[q];
-      if (pc.hist[q] >= 1) dq[VW * 256] += (double)r[q] * (double)in.r1[q];
-      if (pc.hist[q] >= 2) dq[2 * VW * 256] += (double)r[q] * (double)in.r2[q];
+      T *dq = dots + (size_t)q * 256 + threadIdx.x;
+      dq[0] += r[q] * r[q];
+      if (pc.hist[q] >= 1) dq[VW * 256] += r[q] * in.r1[q];
+      if (pc.hist[q] >= 2) dq[2 * VW * 256] += r[q] * in.r2[q];
     }
   }
+}
+
+// the per-thread sums of a sweep kernel in the layout of block_columns
+template <typename T, int VW, int NV, bool AA>
+__device__ __forceinline__ void ppr_gather_parts(const T (&res)[VW], const double (&dm)[VW], const T *dots,
+                                                 double (&part)[NV][VW]) {
+  #pragma unroll
+  for (int q = 0; q < VW; ++q) {
+    part[0][q] = (double)res[q];
+    part[1][q] = dm[q];
+  }
+  if constexpr (AA)
+    #pragma unroll
+    for (int j = 0; j < 3; ++j)
+      #pragma unroll
+      for (int q = 0; q < VW; ++q) part[2 + j][q] = (double)dots[(j * VW + q) * 256 + threadIdx.x];
 }
 
 // Resident blocks per SM the sweep kernel is compiled for (its register
@@ -258,12 +288,14 @@ __global__ void __launch_bounds__(256, ppr_min_blocks<T, AA>()) ppr_spmm_kernel(
   PprCols<VW> pc;
   ppr_cols<VW, AA>(pc, c, col, inv_size, aa);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
-  double part[NV][VW];
+  T res[VW];
+  double dm[VW];
   #pragma unroll
-  for (int j = 0; j < NV; ++j)
-    #pragma unroll
-    for (int q = 0; q < VW; ++q) part[j][q] = 0;
-  __shared__ double dots[AA ? 3 * VW * 256 : 1];
+  for (int q = 0; q < VW; ++q) {
+    res[q] = 0;
+    dm[q] = 0;
+  }
+  __shared__ T dots[AA ? 3 * VW * 256 : 1];
   if (AA)
     for (int j = 0; j < 3 * VW; ++j) dots[j * 256 + threadIdx.x] = 0;
   for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; g < n_items; g += ng) {
@@ -297,14 +329,11 @@ __global__ void __launch_bounds__(256, ppr_min_blocks<T, AA>()) ppr_spmm_kernel(
     } else {
       PprRowIn<T, VW, AA> in;
       ppr_row_in<T, VW, AA>(in, it.x, KT, c, pc, xo, seeds, dmask, rhs, ring);
-      ppr_emit<T, VW, NV, AA>(it.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, part, dots);
+      ppr_emit<T, VW, AA>(it.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, res, dm, dots);
     }
   }
-  if (AA)
-    #pragma unroll
-    for (int j = 0; j < 3; ++j)
-      #pragma unroll
-      for (int q = 0; q < VW; ++q) part[AA ? 2 + j : 0][q] = dots[(j * VW + q) * 256 + threadIdx.x];
+  double part[NV][VW];
+  ppr_gather_parts<T, VW, NV, AA>(res, dm, dots, part);
   block_columns<KT, VW, NV>(part, partials, blockIdx.x);
 }
 
@@ -326,12 +355,14 @@ __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__
   PprCols<VW> pc;
   ppr_cols<VW, AA>(pc, c, col, inv_size, aa);
   const int64_t ng = ((int64_t)gridDim.x * blockDim.x) / G;
-  double part[NV][VW];
+  T res[VW];
+  double dm[VW];
   #pragma unroll
-  for (int j = 0; j < NV; ++j)
-    #pragma unroll
-    for (int q = 0; q < VW; ++q) part[j][q] = 0;
-  __shared__ double dots[AA ? 3 * VW * 256 : 1];
+  for (int q = 0; q < VW; ++q) {
+    res[q] = 0;
+    dm[q] = 0;
+  }
+  __shared__ T dots[AA ? 3 * VW * 256 : 1];
   if (AA)
     for (int j = 0; j < 3 * VW; ++j) dots[j * 256 + threadIdx.x] = 0;
   for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; g < n_crow; g += ng) {
@@ -347,13 +378,10 @@ __global__ void __launch_bounds__(256) ppr_fixup_kernel(const int2 *__restrict__
     }
     PprRowIn<T, VW, AA> in;
     ppr_row_in<T, VW, AA>(in, h.x, KT, c, pc, xo, seeds, dmask, rhs, ring);
-    ppr_emit<T, VW, NV, AA>(h.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, part, dots);
+    ppr_emit<T, VW, AA>(h.x, KT, c, acc, pc, in, xn, beta, rhs != nullptr, ring, res, dm, dots);
   }
-  if (AA)
-    #pragma unroll
-    for (int j = 0; j < 3; ++j)
-      #pragma unroll
-      for (int q = 0; q < VW; ++q) part[AA ? 2 + j : 0][q] = dots[(j * VW + q) * 256 + threadIdx.x];
+  double part[NV][VW];
+  ppr_gather_parts<T, VW, NV, AA>(res, dm, dots, part);
   block_columns<KT, VW, NV>(part, partials, part_base + blockIdx.x);
 }
 
